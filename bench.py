@@ -1,0 +1,343 @@
+"""Benchmark: rays per second of the fused primary + shadow render path.
+
+Workload (one step = one frame): a 512 x 256 x 512 voxel world in 32^3 chunks
+(seeded value-noise fbm terrain + 200 trees), 1920 x 1080 primary rays plus
+one shadow ray per hit toward a seeded sun, reference shading, max 512 steps
+per ray; the step cycles over 8 seeded cameras.  The world is resident in HBM
+before timing (the reference keeps it in persistently mapped buffers too);
+L2 is flushed (256 MiB memset) between steps, outside the timed events.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl ours|reference]
+
+Rank 0 prints one JSON line.  --impl reference times the CPU oracle (a port of
+the reference's traversal; the reference itself is GLSL behind OpenGL and has
+no CPU implementation) on all host cores, on a bounded sample of each frame.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "unnamed-voxel-tracer_gb300"
+
+WORLD = (512, 256, 512)
+IMAGE = (1920, 1080)
+TREES = 200
+SEED = 1
+CAMERAS = 8
+FLUSH_BYTES = 256 << 20
+
+
+def _load(name: str, path: Path):
+    spec = importlib.util.spec_from_file_location(name, path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def workload_config() -> dict:
+    return {"workload": "512x256x512 voxel world (fbm terrain + 200 trees, 32^3 chunks), 1920x1080 primary + "
+                        "1 shadow ray per hit, reference shading, max 512 steps, 8 seeded cameras",
+            "world": list(WORLD), "image": list(IMAGE), "rays": "primary+shadow", "cameras": CAMERAS,
+            "l2": "flushed between steps (256 MiB memset outside the timed events)",
+            "parallelism": "replicas"}
+
+
+def setup_scene(vt, rank: int):
+    desc = vt.gen_desc(WORLD, seed=SEED, trees=TREES)
+    mats = vt.gen_world(desc)
+    cams = [vt.gen_camera(desc, s + CAMERAS * rank, IMAGE[0], IMAGE[1]) for s in range(CAMERAS)]
+    params = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, max_steps=512, shadow_max_steps=512,
+                               sun_dir=vt.gen_sun(SEED))
+    return desc, mats, cams, params
+
+
+def read_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def read_traffic():
+    """DRAM bytes per launch of the render kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "render_traffic.json"
+    if not p.exists():
+        return None, None
+    try:
+        d = json.loads(p.read_text())
+        return float(d["dram_bytes_per_launch"]), d.get("note")
+    except Exception:
+        return None, None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.file:
+            return None
+        self.file.flush()
+        rows = [r.split(", ") for r in Path(self.file.name).read_text().strip().splitlines() if r.strip()]
+        try:
+            os.unlink(self.file.name)
+        except OSError:
+            pass
+        rows = [r for r in rows if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_oracle_sample(vt, oracle_py, mats, cam, params, threads: int, target_s: float):
+    """Rays/s of the CPU oracle on every row_step-th row of one frame, sized to
+    take about target_s seconds.  Returns (rays_per_s, description)."""
+    ow = oracle_py.OracleWorld(mats)
+    pal = vt.default_palette()
+    probe_step = 64
+    t0 = time.perf_counter()
+    _, st = oracle_py.render(ow, pal, cam, params, threads=threads, row_step=probe_step)
+    dt = time.perf_counter() - t0
+    rate = (st["primary_rays"] + st["shadow_rays"]) / max(dt, 1e-6)
+    rays_per_row = (st["primary_rays"] + st["shadow_rays"]) / max(1, (cam.height + probe_step - 1) // probe_step)
+    rows = max(threads, int(rate * target_s / max(rays_per_row, 1.0)))
+    row_step = max(1, cam.height // rows)
+    t0 = time.perf_counter()
+    _, st = oracle_py.render(ow, pal, cam, params, threads=threads, row_step=row_step)
+    dt = time.perf_counter() - t0
+    rays = st["primary_rays"] + st["shadow_rays"]
+    rows_done = (cam.height + row_step - 1) // row_step
+    frame_rays = rays * cam.height / rows_done
+    return rays / dt, (f"every {row_step}th row of a 1920x1080 frame ({st['primary_rays']} primary + "
+                       f"{st['shadow_rays']} shadow rays, {dt:.1f} s)"), frame_rays
+
+
+def run_reference(args, rank: int, world: int) -> None:
+    if rank != 0:
+        return
+    sys.path.insert(0, str(PKG))
+    _load("vt_build", PKG / "build.py").build()
+    import vt
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_py
+    _, mats, cams, params = setup_scene(vt, 0)
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, 20.0 / max(1, args.steps + args.warmup))
+    for i in range(args.warmup):
+        cpu_oracle_sample(vt, oracle_py, mats, cams[i % CAMERAS], params, threads, per_step)
+    rays, secs, descs = 0.0, 0.0, []
+    for i in range(args.steps):
+        r, dsc, frame_rays = cpu_oracle_sample(vt, oracle_py, mats, cams[i % CAMERAS], params, threads, per_step)
+        rays += frame_rays
+        secs += frame_rays / r
+        descs.append(dsc)
+    value = rays / secs / 1e9
+    line = {"impl": "reference", "metric": "Grays/s", "value": value, "unit": "Grays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(),
+            "cpu_baseline": {"value": value, "unit": "Grays/s", "cores": threads, "kind": "port",
+                             "sample": descs[0]},
+            "e2e": {"value": value, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def measure_l2_gbs(torch, dev) -> float:
+    """Read+write GB/s of a 24 MiB copy held in L2 (many passes)."""
+    a = torch.empty(24 << 20, dtype=torch.uint8, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(10):
+        b.copy_(a)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s.record()
+    n = 200
+    for _ in range(n):
+        b.copy_(a)
+    e.record()
+    torch.cuda.synchronize()
+    return 2 * a.numel() * n / (s.elapsed_time(e) * 1e-3) / 1e9
+
+
+def run_ours(args, rank: int, world: int, local_rank: int) -> None:
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    sys.path.insert(0, str(PKG))
+    _load("vt_build", PKG / "build.py").build()
+    import vt
+
+    ctx = vt.Context(local_rank)
+    _, mats, cams, params = setup_scene(vt, rank)
+    wobj = vt.World(ctx, WORLD)
+    wobj.upload_dense(mats)
+    ctx.sync()
+    out = torch.empty(IMAGE[0] * IMAGE[1] * 16, dtype=torch.uint8, device=dev)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+
+    # algorithmic bytes and ray counts per camera (instrumented kernel, untimed)
+    stats = [vt.render_stats(ctx, wobj, c, params, sh) for c in cams]
+    rays = [s["primary_rays"] + s["shadow_rays"] for s in stats]
+    abytes = [8 * s["mask_words"] + 8 * s["coarse_words"] + s["material_bytes"] + s["record_bytes"] for s in stats]
+
+    def frame(i):
+        ctx.check(ctx.lib.vt_render(ctx.handle, wobj.handle, C.byref(cams[i % CAMERAS]), C.byref(params),
+                                    out.data_ptr(), sh))
+
+    for i in range(args.warmup):
+        flush.zero_()
+        frame(i)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            frame(i)
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+    kernel_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(kernel_ms)
+    total_rays = sum(rays[i % CAMERAS] for i in range(args.steps))
+    total_bytes = sum(abytes[i % CAMERAS] for i in range(args.steps))
+    ctx.sync(sh)
+
+    # end to end through the C ABI with host output (pinned), copies inside
+    hbuf = C.c_void_p()
+    nbytes = IMAGE[0] * IMAGE[1] * 16
+    ctx.check(ctx.lib.vt_host_alloc_pinned(ctx.handle, nbytes, C.byref(hbuf)))
+    e2e_s = 0.0
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.check(ctx.lib.vt_render_host(ctx.handle, wobj.handle, C.byref(cams[i % CAMERAS]), C.byref(params),
+                                         hbuf.value))
+        if i >= args.warmup:
+            e2e_s += time.perf_counter() - t0
+    ctx.lib.vt_host_free_pinned(ctx.handle, hbuf)
+
+    t = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms, e2e_s = float(t[0]), float(t[1])
+    value = world * total_rays / (total_ms * 1e-3) / 1e9
+    e2e_value = world * total_rays / e2e_s / 1e9
+
+    if rank != 0:
+        return
+    peak, peak_kind = read_peaks()
+    achieved = total_bytes / (total_ms * 1e-3) / 1e9
+    traffic, traffic_note = read_traffic()
+    l2 = measure_l2_gbs(torch, dev)
+    cpu = None
+    if world == 1:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle_py
+        threads = os.cpu_count() or 1
+        rate, desc, _ = cpu_oracle_sample(vt, oracle_py, mats, cams[0], params, threads, 12.0)
+        cpu = {"value": rate / 1e9, "unit": "Grays/s", "cores": threads, "kind": "port", "sample": desc}
+    name, sms = ctx.device_info()
+    line = {
+        "metric": "Grays/s", "value": value, "unit": "Grays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(),
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes_per_step": total_bytes / args.steps, "traffic_note": traffic_note},
+        "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2,
+                        "peak_kind": "24 MiB device copy held in L2, read+write bytes, this run"},
+        "rays_per_step": total_rays / args.steps,
+        "e2e": {"value": e2e_value, "unit": "Grays/s", "h2d_bytes_per_step": C.sizeof(vt.Camera_t) + C.sizeof(vt.Params_t),
+                "d2h_bytes_per_step": nbytes,
+                "note": "vt_render_host: camera and params travel in the launch; records copied to pinned host memory"},
+        "cpu_baseline": cpu, "clocks": clk.summary(), "device": {"name": name, "sms": sms},
+    }
+    print(json.dumps(line), flush=True)
+    wobj.close()
+    ctx.close()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,260 @@
+/*
+ * vt.h -- C ABI of the GB300 voxel ray-traversal library (libvt.so).
+ *
+ * Plain C99: no CUDA, no C++ and no torch types appear in any signature, so the
+ * header can be consumed unchanged by a C/C++ host, by Python ctypes, or by a
+ * Zig host through @cImport("vt.h").
+ *
+ * The entry points replace the reference engine's render path, which in the
+ * reference is a set of OpenGL objects driven from Zig:
+ *
+ *   world / chunk upload   src/engine/voxel.zig:25-82  (VoxelBrickmap init/set/get/clear/bind)
+ *   model atlas            src/engine/voxel.zig:84-132 (VoxelModelAtlas)
+ *   camera                 src/engine/graphics/camera.zig:5-44 (Camera, UniformData)
+ *   render-frame           src/game.zig:232-256 (primary + secondary dispatch + blit)
+ *   traversal              assets/shaders/map.glsl:83-168 (traceMap)
+ *
+ * Conventions
+ *   - Every call returns vt_status (VT_OK == 0).  On failure a message is kept
+ *     in the context and returned by vt_last_error_string().
+ *   - Handles are opaque, owned by the library and released with *_destroy.
+ *   - Calls that take a vt_stream are asynchronous on that stream (a
+ *     cudaStream_t passed as void*, NULL = the legacy default stream).  Device
+ *     pointers named d_* must be device memory of the context's device.
+ *   - vt_sync() waits for a stream and surfaces the device status word that the
+ *     checked kernels write (VT_ERR_DEVICE_OOB, VT_ERR_TIMEOUT).
+ *   - One vt_ctx per host thread; the library holds no global mutable state
+ *     besides CUDA's own.
+ */
+#ifndef VT_H
+#define VT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VT_ABI_VERSION 1
+
+/* ------------------------------------------------------------------ status */
+typedef int32_t vt_status;
+#define VT_OK              0
+#define VT_ERR_ARG         1  /* bad argument: null pointer, size out of range, bad handle */
+#define VT_ERR_OOM         2  /* device or host allocation failed */
+#define VT_ERR_CUDA        3  /* a CUDA runtime call failed (message has the CUDA error) */
+#define VT_ERR_DEVICE_OOB  4  /* a checked kernel saw an out-of-range index */
+#define VT_ERR_TIMEOUT     5  /* a bounded device-side wait gave up */
+#define VT_ERR_NO_DEVICE   6  /* no CUDA device / driver */
+#define VT_ERR_FORMAT      7  /* malformed input file (.vox) */
+#define VT_ERR_STATE       8  /* call not valid in the object's current state */
+
+typedef struct vt_ctx vt_ctx;
+typedef struct vt_world vt_world;
+typedef struct vt_brickmap vt_brickmap;
+typedef struct vt_batch vt_batch;
+typedef void* vt_stream; /* cudaStream_t */
+
+/* ----------------------------------------------------------------- context */
+int32_t     vt_abi_version(void);
+const char* vt_status_string(vt_status s);
+vt_status   vt_ctx_create(int32_t device, vt_ctx** out);
+vt_status   vt_ctx_destroy(vt_ctx* ctx);
+const char* vt_last_error_string(const vt_ctx* ctx);
+/* Waits for `stream`, then reads and clears the context's device status word. */
+vt_status   vt_sync(vt_ctx* ctx, vt_stream stream);
+/* Device name and SM count of the context's device. */
+vt_status   vt_device_info(vt_ctx* ctx, char* name, int32_t name_len, int32_t* sm_count);
+
+/* Device memory helpers, so that hosts without another CUDA binding (C, Zig,
+ * ctypes) can own frame buffers.  Thin wrappers over the CUDA runtime. */
+vt_status vt_device_alloc(vt_ctx* ctx, size_t nbytes, void** d_ptr);
+vt_status vt_device_free(vt_ctx* ctx, void* d_ptr);
+vt_status vt_host_alloc_pinned(vt_ctx* ctx, size_t nbytes, void** h_ptr);
+vt_status vt_host_free_pinned(vt_ctx* ctx, void* h_ptr);
+vt_status vt_memcpy_h2d(vt_ctx* ctx, void* d_dst, const void* h_src, size_t nbytes, vt_stream stream);
+vt_status vt_memcpy_d2h(vt_ctx* ctx, void* h_dst, const void* d_src, size_t nbytes, vt_stream stream);
+vt_status vt_memset_d(vt_ctx* ctx, void* d_dst, int32_t value, size_t nbytes, vt_stream stream);
+vt_status vt_stream_create(vt_ctx* ctx, vt_stream* out);
+vt_status vt_stream_destroy(vt_ctx* ctx, vt_stream stream);
+
+/* ------------------------------------------------------------------- world
+ * Mode-P world: a dense grid of uint8 materials (0 = air), stored on the device
+ * as 32^3 chunks.  Each chunk holds 8^3 bricks of 4^3 voxels; a brick has one
+ * 64-bit occupancy word (bit = x + 4y + 16z within the brick) and 64 material
+ * bytes; a chunk has one coarse occupancy bit.  Host-side layout of every
+ * dense buffer handed to the library: x fastest, then y, then z
+ * (index = x + X*(y + Y*z)), i.e. the reference's posToIndex order
+ * (src/engine/voxel.zig:21-23).
+ */
+typedef struct {
+    int32_t dims[3]; /* X, Y, Z in voxels, each in [1, 8192], X*Y*Z < 2^32 */
+} vt_world_desc;
+
+typedef struct {
+    int32_t  dims[3];
+    int32_t  chunks[3];        /* chunk counts per axis (dims rounded up to 32) */
+    uint64_t mask_bytes;       /* brick occupancy words */
+    uint64_t material_bytes;   /* chunk-ordered material bytes */
+    uint64_t coarse_bytes;     /* per-chunk occupancy bits */
+    const void* d_mask;        /* device pointers, for inspection */
+    const void* d_materials;
+    const void* d_coarse;
+} vt_world_info;
+
+/* VoxelBrickmap.init (voxel.zig:32-39): an empty world. */
+vt_status vt_world_create(vt_ctx* ctx, const vt_world_desc* desc, vt_world** out);
+vt_status vt_world_destroy(vt_world* world);
+/* VoxelBrickmap.clear (voxel.zig:41-44). */
+vt_status vt_world_clear(vt_world* world, vt_stream stream);
+/* Bulk upload of the whole grid (X*Y*Z bytes, host memory); rebuilds every
+ * brick word and chunk bit on the device.  Replaces the procgen -> set loop
+ * writing into the persistently mapped SSBOs (voxel.zig:58-61). */
+vt_status vt_world_upload_dense(vt_world* world, const uint8_t* h_materials, size_t nbytes, vt_stream stream);
+/* Upload one 32^3 chunk (32768 bytes, x fastest, cells outside dims ignored). */
+vt_status vt_world_upload_chunk(vt_world* world, int32_t cx, int32_t cy, int32_t cz,
+                                const uint8_t* h_chunk, vt_stream stream);
+/* VoxelBrickmap.set / get (voxel.zig:58-70): single voxel write/read. */
+vt_status vt_world_set_voxel(vt_world* world, int32_t x, int32_t y, int32_t z, uint8_t material, vt_stream stream);
+vt_status vt_world_get_voxel(vt_world* world, int32_t x, int32_t y, int32_t z, uint8_t* material);
+/* 256-entry RGBA8 palette (R in the low byte): albedo of each material in the
+ * REFERENCE shading mode (the role of the model atlas texel, map.glsl:57-60). */
+vt_status vt_world_set_palette(vt_world* world, const uint32_t* h_rgba256);
+vt_status vt_world_get_info(const vt_world* world, vt_world_info* info);
+
+/* ------------------------------------------------------------------ camera
+ * Mirrors Camera.UniformData (camera.zig:12-16, camera.glsl:2-6) plus the
+ * target size.  view is row-major as the host math library stores it; with the
+ * shader reading it column-major, a ray's direction is the row vector
+ * (u, v, 1, 1) * view (primary.comp.glsl:39). */
+typedef struct {
+    float   pos[4];       /* ray origin in voxel units (w ignored) */
+    float   view[16];     /* row-major 4x4 */
+    float   fov;          /* field of view across the image width, radians */
+    float   tan_half_fov; /* tan(fov/2), computed by the host (primary.comp.glsl:36) */
+    int32_t width;
+    int32_t height;
+} vt_camera;
+
+/* Camera.set_pos + Camera.rotate + as_uniform_data (camera.zig:18-43) with an
+ * explicit convention: forward = (cos p sin y, sin p, cos p cos y), so a
+ * negative pitch looks down; rows of view are right, up, forward, (0,0,0,1). */
+vt_status vt_camera_look(const float pos[3], float yaw, float pitch, float fov,
+                         int32_t width, int32_t height, vt_camera* out);
+
+/* ---------------------------------------------------------------- render */
+#define VT_RAYS_PRIMARY 1u
+#define VT_RAYS_SHADOW  2u
+#define VT_RAYS_BOUNCE  4u
+
+#define VT_SHADE_NONE      0u /* rgba = palette albedo on hit, 0 on miss */
+#define VT_SHADE_REFERENCE 1u /* primary + secondary + blit arithmetic of the reference */
+#define VT_SHADE_LAMBERT   2u /* palette * albedo * (ambient + diffuse * max(0, n.s) * V) */
+
+#define VT_FLAG_CROSSHAIR 1u  /* blit.fragment.glsl:33 */
+#define VT_FLAG_VIGNETTE  2u  /* blit.fragment.glsl:15-21,34-35 */
+#define VT_FLAG_CHECKED   4u  /* run the bounds-checked kernel variant */
+
+typedef struct {
+    int32_t  max_steps;         /* unit-voxel crossings a primary ray may make, +1 (map.glsl:106) */
+    int32_t  shadow_max_steps;
+    int32_t  bounce_max_steps;
+    uint32_t rays;              /* VT_RAYS_* */
+    uint32_t shade;             /* VT_SHADE_* */
+    uint32_t flags;             /* VT_FLAG_* */
+    uint32_t seed;              /* xor-ed into the per-pixel bounce seed */
+    float    sun_dir[3];        /* shadow ray direction, used as given (camera.glsl:8) */
+    float    ambient;           /* LAMBERT k_a */
+    float    diffuse;           /* LAMBERT k_d */
+    float    bounce_weight;     /* weight of the bounce sky term */
+} vt_params;
+
+/* One record per pixel, 16 bytes. */
+typedef struct {
+    uint32_t voxel;    /* x + X*(y + Y*z) of the hit voxel, 0xFFFFFFFF on miss */
+    float    t;        /* entry distance of the hit voxel along the ray, -1 on miss */
+    uint32_t rgba;     /* shaded colour, RGBA8, R in the low byte */
+    uint8_t  face;     /* 2*axis + (dir[axis] > 0 ? 0 : 1); 0xFF on miss */
+    uint8_t  material; /* material of the hit voxel, 0 on miss */
+    uint8_t  flags;    /* VT_HIT_* */
+    uint8_t  pad;
+} vt_hit;
+
+#define VT_HIT_PRIMARY   1u /* primary ray hit a voxel */
+#define VT_HIT_SHADOWED  2u /* shadow ray hit a voxel */
+#define VT_HIT_BOUNCE    4u /* bounce ray hit a voxel */
+
+void vt_params_default(vt_params* p);
+
+/* Game.render (game.zig:232-256): primary rays, optional shadow and bounce
+ * rays and the shading of primary.comp + secondary.comp + blit.fragment, fused
+ * into one launch.  d_out holds width*height records, row-major, row 0 at
+ * v = -1 (bottom of the image, as the GL image is addressed). */
+vt_status vt_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
+                    const vt_params* params, vt_hit* d_out, vt_stream stream);
+/* Same, with host output: copies the records back and synchronises. */
+vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
+                         const vt_params* params, vt_hit* h_out);
+
+/* Counters of one render, from an instrumented kernel variant.  The byte
+ * counts are algorithmic: 8 per brick word and per coarse word consulted,
+ * 1 per material byte read on a hit, 16 per record stored. */
+typedef struct {
+    uint64_t primary_rays;
+    uint64_t primary_hits;
+    uint64_t shadow_rays;
+    uint64_t shadow_hits;
+    uint64_t bounce_rays;
+    uint64_t bounce_hits;
+    uint64_t mask_words;
+    uint64_t coarse_words;
+    uint64_t material_bytes;
+    uint64_t record_bytes;
+    uint64_t steps;          /* unit-voxel crossings, all rays */
+    uint64_t iterations;     /* traversal loop iterations, all rays */
+} vt_stats;
+vt_status vt_render_stats(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
+                          const vt_params* params, vt_stats* out, vt_stream stream);
+
+/* traceMap over an explicit ray list (map.glsl:83-168 semantics on the mode-P
+ * world, no clipping beyond the grid box): d_origins/d_dirs are n*3 floats. */
+vt_status vt_trace_rays(vt_ctx* ctx, const vt_world* world, const float* d_origins,
+                        const float* d_dirs, int32_t n, int32_t max_steps,
+                        vt_hit* d_out, vt_stream stream);
+
+/* ------------------------------------------------------------- generators
+ * Seeded synthetic scenes (host code, deterministic across machines). */
+typedef struct {
+    int32_t  dims[3];
+    float    base_height;    /* terrain height = base + amplitude * fbm, fbm in [-1, 1] */
+    float    amplitude;
+    float    period;         /* wavelength of the first octave (base frequency 1/period) */
+    float    water_level;    /* air cells with y < water_level above the terrain become water */
+    float    camera_height;  /* cameras sit this far above the terrain or water */
+    int32_t  octaves;        /* lacunarity 2, gain 0.5 */
+    int32_t  trees;          /* trees to plant: trunk 1x6x1 (material 5), 5^3 leaves (6) kept w.p. 0.7 */
+    int32_t  caves;          /* 1 = remove solid cells where 3D value-noise fbm > cave_threshold */
+    float    cave_threshold;
+    float    cave_period;
+    uint64_t seed;
+} vt_gen_desc;
+/* Defaults of the plain terrain generator scaled by `scale` (1.0: base 64,
+ * amplitude 24, period 64, water 56, camera 10 voxels up, 4 octaves). */
+void      vt_gen_desc_init(vt_gen_desc* desc, int32_t x, int32_t y, int32_t z, float scale, uint64_t seed);
+/* Fills h_out (X*Y*Z bytes, x fastest) on `threads` host threads. */
+vt_status vt_gen_world(const vt_gen_desc* desc, uint8_t* h_out, size_t nbytes, int32_t threads);
+/* Terrain height at column (x, z): cells y < height are solid before caves. */
+int32_t   vt_gen_height(const vt_gen_desc* desc, int32_t x, int32_t z);
+/* A seeded pinhole camera camera_height above the terrain at a seeded column,
+ * seeded yaw in [0, 360) degrees and pitch in [-30, 0] degrees, FOV 70 deg. */
+vt_status vt_gen_camera(const vt_gen_desc* desc, uint64_t seed, int32_t width, int32_t height, vt_camera* out);
+/* The default palette (material 0 transparent). */
+vt_status vt_default_palette(uint32_t* h_rgba256);
+/* A seeded sun direction (upper hemisphere). */
+vt_status vt_gen_sun(uint64_t seed, float out[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VT_H */

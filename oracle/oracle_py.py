@@ -1,0 +1,136 @@
+"""ctypes binding of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loaded by tests/, __graft_entry__.smoke() and the CPU-baseline legs of
+bench.py, as the checker and as the timed CPU baseline.  Nothing in the
+library path imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent / "unnamed-voxel-tracer_gb300"))
+import vt  # noqa: E402  (struct layouts of include/vt.h)
+
+import importlib.util  # noqa: E402
+
+_spec = importlib.util.spec_from_file_location("vt_oracle_build", HERE / "build.py")
+_build = importlib.util.module_from_spec(_spec)
+_spec.loader.exec_module(_build)
+
+
+class VtoWorld_t(C.Structure):
+    _fields_ = [("dims", C.c_int32 * 3), ("mats", C.c_void_p), ("chunk_occ", C.c_void_p), ("chunks", C.c_int32 * 3)]
+
+
+class VtoTrace_t(C.Structure):
+    _fields_ = [("hit", C.c_int32), ("voxel", C.c_uint32), ("cell", C.c_int32 * 3), ("t", C.c_float),
+                ("face", C.c_int32), ("axis", C.c_int32), ("material", C.c_uint8), ("steps", C.c_int32),
+                ("mask_words", C.c_uint64), ("coarse_words", C.c_uint64)]
+
+
+class VtoRefWorld_t(C.Structure):
+    _fields_ = [("chunks", C.c_void_p), ("data", C.c_void_p), ("ndata", C.c_uint64), ("atlas", C.c_void_p)]
+
+
+class VtoRefHit_t(C.Structure):
+    _fields_ = [("data", C.c_uint32), ("hit_pos", C.c_float * 3), ("normal", C.c_float * 3),
+                ("iterations", C.c_int32)]
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        lib = C.CDLL(str(_build.build()))
+        P = C.c_void_p
+        lib.vto_world_init.argtypes = [C.POINTER(VtoWorld_t), C.POINTER(C.c_int32), P]
+        lib.vto_world_init.restype = C.c_int32
+        lib.vto_world_free.argtypes = [C.POINTER(VtoWorld_t)]
+        lib.vto_trace_p.argtypes = [C.POINTER(VtoWorld_t), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
+                                    C.POINTER(VtoTrace_t)]
+        lib.vto_render.argtypes = [C.POINTER(VtoWorld_t), P, C.POINTER(vt.Camera_t), C.POINTER(vt.Params_t), P,
+                                   C.c_int32, C.POINTER(vt.Stats_t)]
+        lib.vto_render.restype = C.c_int32
+        lib.vto_render_sampled.argtypes = [C.POINTER(VtoWorld_t), P, C.POINTER(vt.Camera_t),
+                                           C.POINTER(vt.Params_t), P, C.c_int32, C.c_int32, C.POINTER(vt.Stats_t)]
+        lib.vto_render_sampled.restype = C.c_int32
+        lib.vto_trace_rays.argtypes = [C.POINTER(VtoWorld_t), P, P, C.c_int32, C.c_int32, P]
+        lib.vto_sinf.argtypes = [C.c_float]
+        lib.vto_sinf.restype = C.c_float
+        lib.vto_cosf.argtypes = [C.c_float]
+        lib.vto_cosf.restype = C.c_float
+        lib.vto_tracemap.argtypes = [C.POINTER(VtoRefWorld_t), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                     C.c_int32, C.POINTER(VtoRefHit_t)]
+        _lib = lib
+    return _lib
+
+
+class OracleWorld:
+    """A dense mode-P world (uint8 array [z, y, x]) seen by the oracle."""
+
+    def __init__(self, mats: np.ndarray):
+        self.mats = np.ascontiguousarray(mats, dtype=np.uint8)
+        Z, Y, X = self.mats.shape
+        self.dims = (X, Y, Z)
+        self.w = VtoWorld_t()
+        dims = (C.c_int32 * 3)(X, Y, Z)
+        if load().vto_world_init(C.byref(self.w), dims, self.mats.ctypes.data) != 0:
+            raise MemoryError("oracle world init failed")
+
+    def __del__(self):
+        if _lib is not None and getattr(self, "w", None) is not None:
+            _lib.vto_world_free(C.byref(self.w))
+            self.w = None
+
+
+def render(world: OracleWorld, palette: np.ndarray, cam, params, threads: int = 1, row_step: int = 1):
+    """Returns (records[H*W] as vt.HIT_DTYPE, stats dict).  With row_step > 1
+    only rows 0, row_step, 2*row_step, ... are rendered (others stay zero)."""
+    lib = load()
+    out = np.zeros(cam.width * cam.height, dtype=vt.HIT_DTYPE)
+    pal = np.ascontiguousarray(palette, dtype=np.uint32)
+    st = vt.Stats_t()
+    rc = lib.vto_render_sampled(C.byref(world.w), pal.ctypes.data, C.byref(cam), C.byref(params),
+                                out.ctypes.data, threads, row_step, C.byref(st))
+    if rc != 0:
+        raise RuntimeError("oracle render failed")
+    return out, st.as_dict()
+
+
+def trace_rays(world: OracleWorld, origins: np.ndarray, dirs: np.ndarray, max_steps: int) -> np.ndarray:
+    origins = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)
+    dirs = np.ascontiguousarray(dirs, dtype=np.float32).reshape(-1, 3)
+    out = np.zeros(origins.shape[0], dtype=vt.HIT_DTYPE)
+    load().vto_trace_rays(C.byref(world.w), origins.ctypes.data, dirs.ctypes.data, origins.shape[0], max_steps,
+                          out.ctypes.data)
+    return out
+
+
+def trace_one(world: OracleWorld, o, d, max_steps: int) -> VtoTrace_t:
+    tr = VtoTrace_t()
+    load().vto_trace_p(C.byref(world.w), (C.c_float * 3)(*o), (C.c_float * 3)(*d), max_steps, C.byref(tr))
+    return tr
+
+
+class OracleRefWorld:
+    """The reference's world format: 64^3 chunk table, u32 bricks, 256^3 atlas."""
+
+    def __init__(self, chunks: np.ndarray, data: np.ndarray, atlas: np.ndarray):
+        self.chunks = np.ascontiguousarray(chunks, dtype=np.uint32)
+        self.data = np.ascontiguousarray(data, dtype=np.uint32)
+        self.atlas = np.ascontiguousarray(atlas, dtype=np.uint32)
+        assert self.chunks.size == 64 ** 3 and self.atlas.size == 256 ** 3
+        self.w = VtoRefWorld_t(self.chunks.ctypes.data, self.data.ctypes.data, self.data.size, self.atlas.ctypes.data)
+
+
+def tracemap(world: OracleRefWorld, o, d, max_steps: int) -> VtoRefHit_t:
+    h = VtoRefHit_t()
+    load().vto_tracemap(C.byref(world.w), (C.c_float * 3)(*o), (C.c_float * 3)(*d), max_steps, C.byref(h))
+    return h

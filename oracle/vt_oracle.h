@@ -1,0 +1,103 @@
+/*
+ * vt_oracle.h -- CPU oracle for the voxel ray-traversal path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links or calls
+ * this code; only tests/, __graft_entry__.smoke() and the cpu_baseline /
+ * reference arm of bench.py load it, as the checker and as the timed CPU
+ * baseline.  It restates the reference's traversal and shading on the CPU with
+ * plain scalar C (no skipping, no SIMD), compiled with -ffp-contract=off so
+ * that every float operation rounds exactly as written.
+ *
+ * Two traversals:
+ *   mode P  plane-indexed Amanatides-Woo unit-step DDA over a dense uint8 grid,
+ *           with the reference's tie-break chain (map.glsl:158), zero-direction
+ *           fix (map.glsl:85-90), face numbering (map.glsl:119-127) and
+ *           max-step loop (map.glsl:106).
+ *   mode R  traceMap itself (map.glsl:83-168) over the reference's world format
+ *           (64^3 chunk table, 8^3 u32 bricks, 256^3 RGBA8 model atlas).
+ *
+ * Pinning.  The reference ships no golden vectors for this path.  Mode R is
+ * checked bit-for-bit against the reference's own map.glsl compiled as C++
+ * (oracle/build_ref.py -> oracle/_ref), and mode P against that same compiled
+ * traceMap on worlds of full 8^3 models, where both describe the same voxel
+ * DDA (tests/test_oracle_ref.py).
+ */
+#ifndef VT_ORACLE_H
+#define VT_ORACLE_H
+
+#include <stdint.h>
+#include <stddef.h>
+#include "../include/vt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ mode P world */
+typedef struct {
+    int32_t dims[3];
+    const uint8_t* mats;  /* dense, x fastest */
+    /* derived, owned by the oracle (vto_world_init / vto_world_free) */
+    uint8_t* chunk_occ;   /* per 32^3 chunk */
+    int32_t chunks[3];
+} vto_world;
+
+int32_t vto_world_init(vto_world* w, const int32_t dims[3], const uint8_t* mats);
+void    vto_world_free(vto_world* w);
+
+typedef struct {
+    int32_t  hit;
+    uint32_t voxel;      /* linear index or 0xFFFFFFFF */
+    int32_t  cell[3];
+    float    t;
+    int32_t  face;       /* 0..5 or -1 */
+    int32_t  axis;       /* axis of the entry crossing */
+    uint8_t  material;
+    int32_t  steps;      /* unit crossings made */
+    uint64_t mask_words; /* brick words consulted */
+    uint64_t coarse_words;
+} vto_trace;
+
+/* One mode-P ray, unit stepping. */
+void vto_trace_p(const vto_world* w, const float o[3], const float d[3], int32_t max_steps, vto_trace* out);
+
+/* Shading + ray generation for pixel rows [y0, y1) of a frame. */
+void vto_render_rows(const vto_world* w, const uint32_t* palette, const vt_camera* cam,
+                     const vt_params* p, vt_hit* out, int32_t y0, int32_t y1, vt_stats* st);
+/* Whole frame on `threads` POSIX threads (rows interleaved); st may be NULL. */
+int32_t vto_render(const vto_world* w, const uint32_t* palette, const vt_camera* cam,
+                   const vt_params* p, vt_hit* out, int32_t threads, vt_stats* st);
+/* A bounded sample: every `row_step`-th row only (for the timed CPU baseline). */
+int32_t vto_render_sampled(const vto_world* w, const uint32_t* palette, const vt_camera* cam,
+                           const vt_params* p, vt_hit* out, int32_t threads, int32_t row_step,
+                           vt_stats* st);
+
+/* Explicit ray list (same semantics as vt_trace_rays). */
+void vto_trace_rays(const vto_world* w, const float* origins, const float* dirs, int32_t n,
+                    int32_t max_steps, vt_hit* out);
+
+/* The deterministic sine/cosine used for bounce directions. */
+float vto_sinf(float x);
+float vto_cosf(float x);
+
+/* ------------------------------------------------------------ mode R world */
+typedef struct {
+    const uint32_t* chunks; /* 64^3 entries, 0 = empty, else brick index + 1 */
+    const uint32_t* data;   /* bricks, 512 u32 each (Voxel bits) */
+    uint64_t        ndata;  /* number of u32 in data */
+    const uint32_t* atlas;  /* 256^3 RGBA8 texels, x + 256*(y + 256*z) */
+} vto_refworld;
+
+typedef struct {
+    uint32_t data;
+    float    hit_pos[3];
+    float    normal[3];
+    int32_t  iterations;
+} vto_refhit;
+
+void vto_tracemap(const vto_refworld* w, const float o[3], const float d[3], int32_t max_steps, vto_refhit* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

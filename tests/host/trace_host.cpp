@@ -1,0 +1,86 @@
+// Test-only: compiles the device traversal (trace_p.cuh) as host C++ so that
+// its jump logic can be compared with the unit-step oracle without a GPU.
+// The CUDA intrinsics it uses are given their IEEE host equivalents.
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+#include <limits.h>
+#include <algorithm>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+using std::max;
+using std::min;
+static inline float __fmaf_rn(float a, float b, float c) { return fmaf(a, b, c); }
+static inline float __frcp_rn(float x) { return 1.0f / x; }
+static inline float __fmul_rn(float a, float b) { return a * b; }
+static inline float __int2float_rn(int k) { return (float)k; }
+static inline int __float2int_rd(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483647.0f) return INT_MAX;
+    if (x <= -2147483648.0f) return INT_MIN;
+    return (int)floorf(x);
+}
+template <class T> static inline T __ldg(const T* p) { return *p; }
+static inline unsigned atomicOr(unsigned* p, unsigned v) { unsigned o = *p; *p |= v; return o; }
+
+#include "../../unnamed-voxel-tracer_gb300/csrc/trace_p.cuh"
+
+extern "C" int ht_trace_rays(const int32_t dims[3], const uint8_t* dense, const float* origins, const float* dirs,
+                             int32_t n, int32_t max_steps, uint32_t* out /* n * 4 u32, vt_hit layout */,
+                             uint64_t* counters /* mask, coarse */) {
+    vt::WorldView w;
+    int cd[3];
+    for (int i = 0; i < 3; ++i) {
+        w.dims[i] = dims[i];
+        cd[i] = w.cdim[i] = (dims[i] + 31) / 32;
+    }
+    const size_t nch = (size_t)cd[0] * cd[1] * cd[2];
+    std::vector<unsigned long long> mask(nch * 512, 0ull), coarse((nch + 63) / 64, 0ull);
+    std::vector<unsigned char> mats(nch * 32768, 0);
+    for (int z = 0; z < dims[2]; ++z)
+        for (int y = 0; y < dims[1]; ++y)
+            for (int x = 0; x < dims[0]; ++x) {
+                unsigned char m = dense[(size_t)x + (size_t)dims[0] * ((size_t)y + (size_t)dims[1] * z)];
+                if (!m) continue;
+                size_t ci = (size_t)(x >> 5) + cd[0] * ((size_t)(y >> 5) + (size_t)cd[1] * (z >> 5));
+                unsigned bi = ((x >> 2) & 7) | (((y >> 2) & 7) << 3) | (((z >> 2) & 7) << 6);
+                unsigned vb = (x & 3) | ((y & 3) << 2) | ((z & 3) << 4);
+                mask[ci * 512 + bi] |= 1ull << vb;
+                mats[(ci * 512 + bi) * 64 + vb] = m;
+                coarse[ci >> 6] |= 1ull << (ci & 63);
+            }
+    w.mask = mask.data();
+    w.mats = mats.data();
+    w.coarse = coarse.data();
+    w.palette = nullptr;
+    w.nwords = (unsigned)(nch * 512);
+    w.ncoarse = (unsigned)coarse.size();
+    unsigned status = 0;
+    for (int i = 0; i < n; ++i) {
+        vt::PRay r;
+        vt::pray_init(r, origins + 3 * i, dirs + 3 * i);
+        vt::TraceHit h;
+        vt::TraceCounters cnt;
+        bool hit = vt::trace_p<true, true, true>(w, vt::CoarseGlobal{w.coarse}, r, max_steps, h, cnt, &status);
+        uint32_t* o = out + 4 * i;
+        if (hit) {
+            const int e = h.axis;
+            const bool pe = r.pos[e];
+            o[0] = (uint32_t)h.c[0] + (uint32_t)dims[0] * ((uint32_t)h.c[1] + (uint32_t)dims[1] * (uint32_t)h.c[2]);
+            memcpy(&o[1], &h.t, 4);
+            o[2] = cnt.steps;
+            o[3] = (2u * e + (pe ? 0u : 1u)) | (h.mat << 8) | (1u << 16);
+        } else {
+            float mt = -1.0f;
+            o[0] = 0xFFFFFFFFu;
+            memcpy(&o[1], &mt, 4);
+            o[2] = 0;
+            o[3] = 0xFFu;
+        }
+        counters[0] += cnt.mask;
+        counters[1] += cnt.coarse;
+    }
+    return (int)status;
+}

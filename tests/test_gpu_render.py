@@ -1,0 +1,172 @@
+"""CUDA path vs the CPU oracle, through the C ABI (needs a GPU).
+
+Bar: hit voxel, entry face, material, flags and t bit-exact; shaded RGBA8
+within 1/255 per channel (the only float code outside the traversal whose
+rounding may differ is powf in the vignette).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RGB_TOL = 1  # units of 1/255
+
+
+def compare(gpu, ref, rgb_tol=RGB_TOL):
+    assert gpu.shape == ref.shape
+    for f in ("voxel", "face", "material", "flags"):
+        bad = np.flatnonzero(gpu[f] != ref[f])
+        assert bad.size == 0, f"{f}: {bad.size} mismatches, first at {bad[:5]}: gpu {gpu[bad[:5]]} ref {ref[bad[:5]]}"
+    bad = np.flatnonzero(gpu["t"].view(np.uint32) != ref["t"].view(np.uint32))
+    assert bad.size == 0, f"t: {bad.size} mismatches, first {gpu['t'][bad[:5]]} vs {ref['t'][bad[:5]]}"
+    g = gpu["rgba"].view(np.uint8).reshape(-1, 4).astype(np.int16)
+    r = ref["rgba"].view(np.uint8).reshape(-1, 4).astype(np.int16)
+    assert np.abs(g - r).max(initial=0) <= rgb_tol
+
+
+def make_world(vt, ctx, mats):
+    Z, Y, X = mats.shape
+    w = vt.World(ctx, (X, Y, Z))
+    w.upload_dense(mats)
+    return w
+
+
+def render_both(vt, oracle, ctx, mats, cam, params, threads=8):
+    w = make_world(vt, ctx, mats)
+    try:
+        gpu = vt.render_host(ctx, w, cam, params)
+    finally:
+        w.close()
+    ref, stats = oracle.render(oracle.OracleWorld(mats), vt.default_palette(), cam, params, threads=threads)
+    return gpu, ref, stats
+
+
+def random_rays(rng, dims, n):
+    X, Y, Z = dims
+    o = np.stack([rng.uniform(-8, X + 8, n), rng.uniform(-8, Y + 8, n), rng.uniform(-8, Z + 8, n)], 1)
+    d = rng.normal(size=(n, 3))
+    d[rng.random(n) < 0.1, 0] = 0.0          # zero components
+    d[rng.random(n) < 0.1, 1] = 0.0
+    k = rng.random(n) < 0.05                 # axis-aligned diagonals (exact ties)
+    d[k] = np.sign(d[k]) + (d[k] == 0)
+    return o.astype(np.float32), d.astype(np.float32)
+
+
+def test_trace_rays_random_padded_world(vt, oracle, ctx):
+    """Ray list on a world whose dims are not multiples of the 32-voxel chunk."""
+    d = vt.gen_desc((90, 70, 100), scale=0.6, seed=5, trees=20, caves=True)
+    mats = vt.gen_world(d)
+    w = make_world(vt, ctx, mats)
+    rng = np.random.default_rng(1)
+    o, dirs = random_rays(rng, (90, 70, 100), 20000)
+    for steps in (1, 7, 64, 4096):
+        gpu = vt.trace_rays(ctx, w, o, dirs, steps)
+        ref = oracle.trace_rays(oracle.OracleWorld(mats), o, dirs, steps)
+        compare(gpu, ref, rgb_tol=0)  # rgba carries the crossing count here
+    w.close()
+
+
+def test_trace_rays_kat(vt, oracle, ctx):
+    mats = np.zeros((32, 32, 32), dtype=np.uint8)
+    for (x, y, z) in ((10, 5, 7), (0, 1, 0), (0, 1, 1), (1, 1, 1), (0, 5, 7), (4, 0, 4)):
+        mats[z, y, x] = 3
+    o = np.array([(0.5, 5.5, 7.5), (20.5, 5.5, 7.5), (0.5, 0.5, 0.5), (0.5, 0.5, 0.5), (0.5, 0.5, 0.5),
+                  (10.25, 5.5, 7.5), (-3.5, 5.5, 7.5), (4.5, -2.0, 4.5), (-5, 50, 5)], np.float32)
+    d = np.array([(1, 0, 0), (-1, 0, 0), (1, 1, 0), (1, 1, 1), (0, 0, 0), (-1, .2, .3), (1, 0, 0), (0, 1, 0),
+                  (0, 1, 0)], np.float32)
+    w = make_world(vt, ctx, mats)
+    for steps in (2, 10, 11, 512):
+        compare(vt.trace_rays(ctx, w, o, d, steps), oracle.trace_rays(oracle.OracleWorld(mats), o, d, steps),
+                rgb_tol=0)
+    w.close()
+
+
+@pytest.mark.parametrize("shade", ["none", "reference"])
+def test_config0_frame(vt, oracle, ctx, shade):
+    """128^3 terrain, 640x360, primary rays, max 512 steps."""
+    d = vt.gen_desc((128, 128, 128), seed=0)
+    mats = vt.gen_world(d)
+    cam = vt.gen_camera(d, 0, 640, 360)
+    p = vt.default_params(rays=vt.RAYS_PRIMARY, max_steps=512,
+                          shade=vt.SHADE_NONE if shade == "none" else vt.SHADE_REFERENCE)
+    gpu, ref, _ = render_both(vt, oracle, ctx, mats, cam, p)
+    compare(gpu, ref)
+    assert (gpu["flags"] & vt.HIT_PRIMARY).mean() > 0.3
+
+
+def test_config1_world_primary_shadow(vt, oracle, ctx):
+    """512x256x512 with 200 trees; primary + shadow, reference shading
+    (reduced image so the oracle finishes in seconds)."""
+    d = vt.gen_desc((512, 256, 512), seed=1, trees=200)
+    mats = vt.gen_world(d)
+    sun = vt.gen_sun(1)
+    for cs in range(3):
+        cam = vt.gen_camera(d, cs, 320, 180)
+        p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=sun)
+        gpu, ref, _ = render_both(vt, oracle, ctx, mats, cam, p)
+        compare(gpu, ref)
+
+
+def test_bounce_rays(vt, oracle, ctx):
+    d = vt.gen_desc((256, 128, 256), seed=2, trees=60, caves=True)
+    mats = vt.gen_world(d)
+    cam = vt.gen_camera(d, 4, 256, 144)
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW | vt.RAYS_BOUNCE, seed=1234, sun_dir=vt.gen_sun(2))
+    gpu, ref, _ = render_both(vt, oracle, ctx, mats, cam, p)
+    compare(gpu, ref)
+    assert (gpu["flags"] & vt.HIT_BOUNCE).any()
+
+
+def test_lambert_and_checked_variant(vt, oracle, ctx):
+    d = vt.gen_desc((128, 96, 160), seed=9, trees=15)
+    mats = vt.gen_world(d)
+    cam = vt.gen_camera(d, 1, 200, 120)
+    p = vt.default_params(shade=vt.SHADE_LAMBERT, flags=vt.FLAG_CHECKED, sun_dir=vt.gen_sun(9))
+    gpu, ref, _ = render_both(vt, oracle, ctx, mats, cam, p)
+    compare(gpu, ref)
+
+
+def test_stats_match_oracle_counters(vt, oracle, ctx):
+    """Algorithmic byte counters of the instrumented kernel equal the oracle's."""
+    d = vt.gen_desc((256, 128, 256), seed=4, trees=50)
+    mats = vt.gen_world(d)
+    cam = vt.gen_camera(d, 2, 240, 135)
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW | vt.RAYS_BOUNCE, sun_dir=vt.gen_sun(4))
+    w = make_world(vt, ctx, mats)
+    st = vt.render_stats(ctx, w, cam, p)
+    w.close()
+    _, ref = oracle.render(oracle.OracleWorld(mats), vt.default_palette(), cam, p, threads=8)
+    for k in ("primary_rays", "primary_hits", "shadow_rays", "shadow_hits", "bounce_rays", "bounce_hits",
+              "mask_words", "coarse_words", "material_bytes", "record_bytes", "steps"):
+        assert st[k] == ref[k], (k, st[k], ref[k])
+
+
+def test_world_edits_match_oracle(vt, oracle, ctx):
+    """set / get / upload_chunk (VoxelBrickmap.set/get, voxel.zig:58-70)."""
+    d = vt.gen_desc((96, 64, 96), scale=0.5, seed=6, trees=10)
+    mats = vt.gen_world(d)
+    w = make_world(vt, ctx, mats)
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        x, y, z = rng.integers(0, 96), rng.integers(0, 64), rng.integers(0, 96)
+        m = int(rng.integers(0, 7)) if rng.random() < 0.5 else 0
+        w.set(int(x), int(y), int(z), m)
+        mats[z, y, x] = m
+    chunk = rng.integers(0, 3, size=(32, 32, 32)).astype(np.uint8) * (rng.random((32, 32, 32)) < 0.1)
+    w.upload_chunk(1, 0, 2, chunk)
+    mats[64:96, 0:32, 32:64] = chunk
+    empty = np.zeros((32, 32, 32), np.uint8)
+    w.upload_chunk(0, 1, 0, empty)
+    mats[0:32, 32:64, 0:32] = 0
+    for (x, y, z) in ((5, 5, 5), (40, 10, 70), (95, 63, 95)):
+        assert w.get(x, y, z) == mats[z, y, x]
+    cam = vt.gen_camera(d, 3, 160, 90)
+    p = vt.default_params()
+    gpu = vt.render_host(ctx, w, cam, p)
+    ref, _ = oracle.render(oracle.OracleWorld(mats), vt.default_palette(), cam, p, threads=8)
+    compare(gpu, ref)
+    w.clear()
+    ctx.sync()
+    gpu = vt.render_host(ctx, w, cam, p)
+    assert not (gpu["flags"] & vt.HIT_PRIMARY).any()
+    w.close()

@@ -1,0 +1,189 @@
+// api.cu -- context, status and device-memory entry points of the C ABI.
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "vt_internal.h"
+
+namespace vt {
+
+vt_status fail(vt_ctx* ctx, vt_status s, const std::string& msg, cudaError_t err) {
+    if (ctx) {
+        ctx->last_error = msg;
+        if (err != cudaSuccess) {
+            ctx->last_error += ": ";
+            ctx->last_error += cudaGetErrorString(err);
+        }
+    }
+    return s;
+}
+
+vt_status check_cuda(vt_ctx* ctx, cudaError_t err, const char* what) {
+    if (err == cudaSuccess) return VT_OK;
+    vt_status s = VT_ERR_CUDA;
+    if (err == cudaErrorMemoryAllocation) s = VT_ERR_OOM;
+    if (err == cudaErrorNoDevice || err == cudaErrorInsufficientDriver) s = VT_ERR_NO_DEVICE;
+    return fail(ctx, s, what, err);
+}
+
+vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out) {
+    if (bytes > ctx->scratch_bytes) {
+        if (ctx->d_scratch) {
+            VT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            cudaFree(ctx->d_scratch);
+            ctx->d_scratch = nullptr;
+            ctx->scratch_bytes = 0;
+        }
+        VT_CUDA(ctx, cudaMalloc(&ctx->d_scratch, bytes));
+        ctx->scratch_bytes = bytes;
+    }
+    *out = ctx->d_scratch;
+    return VT_OK;
+}
+
+}  // namespace vt
+
+using namespace vt;
+
+extern "C" {
+
+int32_t vt_abi_version(void) { return VT_ABI_VERSION; }
+
+const char* vt_status_string(vt_status s) {
+    switch (s) {
+        case VT_OK: return "ok";
+        case VT_ERR_ARG: return "invalid argument";
+        case VT_ERR_OOM: return "out of memory";
+        case VT_ERR_CUDA: return "CUDA error";
+        case VT_ERR_DEVICE_OOB: return "device index out of range";
+        case VT_ERR_TIMEOUT: return "device wait timed out";
+        case VT_ERR_NO_DEVICE: return "no CUDA device";
+        case VT_ERR_FORMAT: return "malformed input";
+        case VT_ERR_STATE: return "invalid state";
+        default: return "unknown status";
+    }
+}
+
+vt_status vt_ctx_create(int32_t device, vt_ctx** out) {
+    if (!out) return VT_ERR_ARG;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return VT_ERR_NO_DEVICE;
+    if (device < 0 || device >= count) return VT_ERR_ARG;
+    vt_ctx* ctx = new (std::nothrow) vt_ctx();
+    if (!ctx) return VT_ERR_OOM;
+    ctx->device = device;
+    vt_status s = VT_OK;
+    do {
+        if ((e = cudaSetDevice(device)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaSetDevice"); break; }
+        cudaDeviceProp prop;
+        if ((e = cudaGetDeviceProperties(&prop, device)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaGetDeviceProperties"); break; }
+        std::snprintf(ctx->name, sizeof(ctx->name), "%s", prop.name);
+        ctx->sm_count = prop.multiProcessorCount;
+        if ((e = cudaMalloc(&ctx->d_status, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
+        if ((e = cudaMemset(ctx->d_status, 0, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMemset"); break; }
+        if ((e = cudaMalloc(&ctx->d_counters, kNumCounters * sizeof(unsigned long long))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
+        if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaStreamCreate"); break; }
+    } while (0);
+    if (s != VT_OK) {
+        vt_ctx_destroy(ctx);
+        return s;
+    }
+    *out = ctx;
+    return VT_OK;
+}
+
+vt_status vt_ctx_destroy(vt_ctx* ctx) {
+    if (!ctx) return VT_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->d_scratch) cudaFree(ctx->d_scratch);
+    if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return VT_OK;
+}
+
+const char* vt_last_error_string(const vt_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+vt_status vt_sync(vt_ctx* ctx, vt_stream stream) {
+    if (!ctx) return VT_ERR_ARG;
+    VT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+    unsigned st = 0;
+    VT_CUDA(ctx, cudaMemcpy(&st, ctx->d_status, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st) {
+        VT_CUDA(ctx, cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
+        if (st & kStatusOob) return fail(ctx, VT_ERR_DEVICE_OOB, "a checked kernel saw an out-of-range index");
+        return fail(ctx, VT_ERR_TIMEOUT, "a bounded device wait gave up");
+    }
+    return VT_OK;
+}
+
+vt_status vt_device_info(vt_ctx* ctx, char* name, int32_t name_len, int32_t* sm_count) {
+    if (!ctx) return VT_ERR_ARG;
+    if (name && name_len > 0) std::snprintf(name, (size_t)name_len, "%s", ctx->name);
+    if (sm_count) *sm_count = ctx->sm_count;
+    return VT_OK;
+}
+
+vt_status vt_device_alloc(vt_ctx* ctx, size_t nbytes, void** d_ptr) {
+    if (!ctx || !d_ptr) return VT_ERR_ARG;
+    *d_ptr = nullptr;
+    VT_CUDA(ctx, cudaMalloc(d_ptr, nbytes ? nbytes : 1));
+    return VT_OK;
+}
+
+vt_status vt_device_free(vt_ctx* ctx, void* d_ptr) {
+    if (!ctx) return VT_ERR_ARG;
+    VT_CUDA(ctx, cudaFree(d_ptr));
+    return VT_OK;
+}
+
+vt_status vt_host_alloc_pinned(vt_ctx* ctx, size_t nbytes, void** h_ptr) {
+    if (!ctx || !h_ptr) return VT_ERR_ARG;
+    *h_ptr = nullptr;
+    VT_CUDA(ctx, cudaMallocHost(h_ptr, nbytes ? nbytes : 1));
+    return VT_OK;
+}
+
+vt_status vt_host_free_pinned(vt_ctx* ctx, void* h_ptr) {
+    if (!ctx) return VT_ERR_ARG;
+    VT_CUDA(ctx, cudaFreeHost(h_ptr));
+    return VT_OK;
+}
+
+vt_status vt_memcpy_h2d(vt_ctx* ctx, void* d_dst, const void* h_src, size_t nbytes, vt_stream stream) {
+    if (!ctx || (nbytes && (!d_dst || !h_src))) return VT_ERR_ARG;
+    VT_CUDA(ctx, cudaMemcpyAsync(d_dst, h_src, nbytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    return VT_OK;
+}
+
+vt_status vt_memcpy_d2h(vt_ctx* ctx, void* h_dst, const void* d_src, size_t nbytes, vt_stream stream) {
+    if (!ctx || (nbytes && (!d_src || !h_dst))) return VT_ERR_ARG;
+    VT_CUDA(ctx, cudaMemcpyAsync(h_dst, d_src, nbytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    return VT_OK;
+}
+
+vt_status vt_memset_d(vt_ctx* ctx, void* d_dst, int32_t value, size_t nbytes, vt_stream stream) {
+    if (!ctx || (nbytes && !d_dst)) return VT_ERR_ARG;
+    VT_CUDA(ctx, cudaMemsetAsync(d_dst, value, nbytes, (cudaStream_t)stream));
+    return VT_OK;
+}
+
+vt_status vt_stream_create(vt_ctx* ctx, vt_stream* out) {
+    if (!ctx || !out) return VT_ERR_ARG;
+    cudaStream_t s = nullptr;
+    VT_CUDA(ctx, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    *out = (vt_stream)s;
+    return VT_OK;
+}
+
+vt_status vt_stream_destroy(vt_ctx* ctx, vt_stream stream) {
+    if (!ctx) return VT_ERR_ARG;
+    VT_CUDA(ctx, cudaStreamDestroy((cudaStream_t)stream));
+    return VT_OK;
+}
+
+}  // extern "C"

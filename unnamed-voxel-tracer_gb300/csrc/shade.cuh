@@ -1,0 +1,217 @@
+// shade.cuh -- ray generation and shading on the device (mode P).
+//
+//   primary ray     primary.comp.glsl:31-39 (direction normalised in 3-D)
+//   sky             camera.glsl:11-19 (SkyDome2, sun as a parameter, integer
+//                   powers as products)
+//   shadow origin   secondary.comp.glsl:37 (hit point + normal * 0.001)
+//   illumination    secondary.comp.glsl:45-48 stored in RGBA8 (gbuffer.zig:13)
+//   composite       blit.fragment.glsl:15-35 (illum.a * sky, crosshair, vignette)
+//   bounce          rng.glsl:16-29,41-55 (wang_hash, CosineSampleHemisphere),
+//                   per-pixel seed x*1973 + y*9277 (primary.comp.glsl:25)
+//
+// Compiled with --fmad=false: every expression rounds as written.
+#pragma once
+
+#include "vt_internal.h"
+
+namespace vt {
+
+// Camera and parameters of one frame, by value in kernel parameter space.
+struct FrameParams {
+    float pos[3];
+    float view[16];
+    float tan_half_fov;
+    int width, height;
+    int max_steps, shadow_max_steps, bounce_max_steps;
+    unsigned rays, shade, flags, seed;
+    float sun[3];
+    float ambient, diffuse, bounce_weight;
+};
+
+__device__ __forceinline__ void primary_ray(const FrameParams& f, int px, int py, float o[3], float d[3]) {
+    const float W = (float)f.width, H = (float)f.height;
+    float u = (((float)px / W) * 2.0f) - 1.0f;
+    float v = (((float)py / H) * 2.0f) - 1.0f;
+    v = v * (H / W);
+    u = u * f.tan_half_fov;
+    v = v * f.tan_half_fov;
+    float q[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) q[j] = ((u * f.view[0 * 4 + j] + v * f.view[1 * 4 + j]) + f.view[2 * 4 + j]) + f.view[3 * 4 + j];
+    const float len = __fsqrt_rn((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        d[j] = __fdiv_rn(q[j], len);
+        o[j] = f.pos[j];
+    }
+}
+
+__device__ __forceinline__ float clampf(float x, float a, float b) { return x < a ? a : (x > b ? b : x); }
+
+__device__ __forceinline__ unsigned unorm8(float x) { return (unsigned)__float2int_rn(clampf(x, 0.0f, 1.0f) * 255.0f); }
+
+__device__ __forceinline__ float dot3(const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+__device__ __forceinline__ void normalize3(const float a[3], float o[3]) {
+    const float len = __fsqrt_rn(dot3(a, a));
+    o[0] = __fdiv_rn(a[0], len);
+    o[1] = __fdiv_rn(a[1], len);
+    o[2] = __fdiv_rn(a[2], len);
+}
+
+__device__ __forceinline__ void sky(const float sun[3], const float rd[3], float col[3]) {
+    float sn[3], rn[3];
+    normalize3(sun, sn);
+    normalize3(rd, rn);
+    const float s = clampf(dot3(sn, rn), 0.0f, 1.2f);
+    const float s2 = s * s, s3 = s2 * s, s4 = s2 * s2, s8 = s4 * s4;
+    const float dy = rd[1] * 0.2f;
+    col[0] = ((0.6f - dy * 1.0f) + (0.15f * 0.5f)) + (0.4f * 1.0f) * s8 + 0.2f * s3;
+    col[1] = ((0.71f - dy * 0.5f) + (0.15f * 0.5f)) + (0.4f * 0.6f) * s8 + 0.08f * s3;
+    col[2] = ((0.75f - dy * 1.0f) + (0.15f * 0.5f)) + (0.4f * 0.1f) * s8 + 0.04f * s3;
+}
+
+__device__ __forceinline__ float vignette(int px, int py, int W, int H) {
+    const float u = ((float)px + 0.5f) / (float)W;
+    const float v = ((float)py + 0.5f) / (float)H;
+    const float a = u * (1.0f - u), b = v * (1.0f - v);
+    return powf(a * b * 15.0f, 0.18f);
+}
+
+__device__ __forceinline__ bool crosshair(int px, int py, int W, int H) {
+    const float u = ((float)px + 0.5f) / (float)W - 0.5f;
+    const float v = ((float)py + 0.5f) / (float)H - 0.5f;
+    return __fsqrt_rn(u * u + v * v) <= 0.002f;
+}
+
+__device__ __forceinline__ unsigned wang_hash(unsigned& seed) {
+    unsigned s = (seed ^ 61u) ^ (seed >> 16);
+    s *= 9u;
+    s = s ^ (s >> 4);
+    s *= 0x27d4eb2du;
+    s = s ^ (s >> 15);
+    seed = s;
+    return s;
+}
+
+__device__ __forceinline__ float rand01(unsigned& seed) { return __uint2float_rn(wang_hash(seed)) * 0x1p-32f; }
+
+// Deterministic sine/cosine: Cody-Waite reduction by pi/2 split into three
+// floats (1.5703125 + 0x1.fb4p-12 + 0x1.4442d2p-24, each the leading bits of
+// the remainder of the previous split) and Taylor polynomials of degree 9 (sin)
+// and 10 (cos) on |r| <= pi/4, evaluated with correctly rounded fma.
+__device__ __forceinline__ void det_sincos(float x, float& s, float& c) {
+    const float k = rintf(x * 0x1.45f306p-1f);
+    float r = __fmaf_rn(-k, 0x1.92p+0f, x);
+    r = __fmaf_rn(-k, 0x1.fb4p-12f, r);
+    r = __fmaf_rn(-k, 0x1.4442d2p-24f, r);
+    const float r2 = r * r;
+    float ps = __fmaf_rn(r2, 1.0f / 362880.0f, -1.0f / 5040.0f);
+    ps = __fmaf_rn(r2, ps, 1.0f / 120.0f);
+    ps = __fmaf_rn(r2, ps, -1.0f / 6.0f);
+    ps = __fmaf_rn(r2 * r, ps, r);
+    float pc = __fmaf_rn(r2, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+    pc = __fmaf_rn(r2, pc, -1.0f / 720.0f);
+    pc = __fmaf_rn(r2, pc, 1.0f / 24.0f);
+    pc = __fmaf_rn(r2, pc, -0.5f);
+    pc = __fmaf_rn(r2, pc, 1.0f);
+    const int q = ((int)k) & 3;
+    if (q == 0) { s = ps; c = pc; }
+    else if (q == 1) { s = pc; c = -ps; }
+    else if (q == 2) { s = -ps; c = -pc; }
+    else { s = -pc; c = ps; }
+}
+
+__device__ __forceinline__ void cross3(const float a[3], const float b[3], float o[3]) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+__device__ __forceinline__ void cosine_hemisphere(const float n[3], unsigned& seed, float out[3]) {
+    const float u1 = rand01(seed), u2 = rand01(seed);
+    const float r = __fsqrt_rn(u1);
+    const float theta = 6.28f * u2;
+    const float up[3] = {0.0f, 1.0f, 1.0f};
+    float b0[3], B[3], T[3];
+    cross3(n, up, b0);
+    normalize3(b0, B);
+    cross3(B, n, T);
+    float st, ct;
+    det_sincos(theta, st, ct);
+    const float rs = r * st, rc = r * ct, h = __fsqrt_rn(1.0f - u1);
+    float v[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) v[j] = (rs * B[j] + h * n[j]) + rc * T[j];
+    normalize3(v, out);
+}
+
+// Colour of a primary hit in REFERENCE / LAMBERT / NONE shading.
+__device__ __forceinline__ void shade_hit(const FrameParams& f, unsigned alb, int axis, bool pos_axis, bool shadowed,
+                                          bool bounce_open, const float bdir[3], float col[4]) {
+    float albf[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) albf[j] = (float)((alb >> (8 * j)) & 255u) / 255.0f;
+    if (f.shade == VT_SHADE_REFERENCE) {
+        const float a = shadowed ? 0.0f : (float)unorm8(0.3f) / 255.0f;
+        float sq[3], sc[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) sq[j] = (float)unorm8(f.sun[j]) / 255.0f;
+        sky(f.sun, sq, sc);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) col[j] = albf[j] + a * sc[j];
+        col[3] = albf[3] + a * 1.0f;
+        if (bounce_open) {
+            float bc[3];
+            sky(f.sun, bdir, bc);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) col[j] = col[j] + f.bounce_weight * (albf[j] * bc[j]);
+        }
+    } else if (f.shade == VT_SHADE_LAMBERT) {
+        float sn[3], nrm[3] = {0.0f, 0.0f, 0.0f};
+        nrm[0] = axis == 0 ? (pos_axis ? -1.0f : 1.0f) : 0.0f;
+        nrm[1] = axis == 1 ? (pos_axis ? -1.0f : 1.0f) : 0.0f;
+        nrm[2] = axis == 2 ? (pos_axis ? -1.0f : 1.0f) : 0.0f;
+        normalize3(f.sun, sn);
+        float ndl = dot3(nrm, sn);
+        if (ndl < 0.0f) ndl = 0.0f;
+        const float vis = shadowed ? 0.0f : 1.0f;
+        const float k = f.ambient + f.diffuse * ndl * vis;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) col[j] = albf[j] * k;
+        col[3] = 1.0f;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) col[j] = albf[j];
+    }
+}
+
+__device__ __forceinline__ void shade_miss(const FrameParams& f, const float d[3], float col[4]) {
+    col[0] = col[1] = col[2] = col[3] = 0.0f;
+    if (f.shade == VT_SHADE_REFERENCE) {
+        float sc[3];
+        sky(f.sun, d, sc);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) col[j] = (float)unorm8(sc[j]) / 255.0f;
+        col[3] = 1.0f;
+    }
+}
+
+__device__ __forceinline__ unsigned composite(const FrameParams& f, int px, int py, float col[4]) {
+    if (f.shade == VT_SHADE_REFERENCE) {
+        if ((f.flags & VT_FLAG_CROSSHAIR) && crosshair(px, py, f.width, f.height)) {
+            col[0] = col[0] * 0.5f + 0.5f;
+            col[1] = col[1] * 0.5f + 0.5f;
+            col[2] = col[2] * 0.5f + 0.5f;
+            col[3] = col[3] * 0.5f + 0.2f;
+        }
+        if (f.flags & VT_FLAG_VIGNETTE) {
+            const float g = vignette(px, py, f.width, f.height);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) col[j] = g * col[j];
+        }
+    }
+    return unorm8(col[0]) | (unorm8(col[1]) << 8) | (unorm8(col[2]) << 16) | (unorm8(col[3]) << 24);
+}
+
+}  // namespace vt

@@ -1,0 +1,93 @@
+// vt_internal.h -- private structures of libvt (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/vt.h"
+
+namespace vt {
+
+constexpr int kChunk = 32;          // chunk edge in voxels
+constexpr int kBrick = 4;           // brick edge in voxels
+constexpr int kBricksPerChunk = 512;
+constexpr int kChunkBytes = kChunk * kChunk * kChunk;
+
+// Error bits of the device status word.
+constexpr unsigned kStatusOob = 1u;
+constexpr unsigned kStatusTimeout = 2u;
+
+// Device counters written by the instrumented kernels (order = vt_stats).
+constexpr int kNumCounters = 12;
+
+// Everything a traversal kernel needs to read a mode-P world.
+struct WorldView {
+    const unsigned long long* mask;     // brick occupancy words, chunk-major
+    const unsigned char* mats;          // 64 material bytes per brick, same order
+    const unsigned long long* coarse;   // one bit per chunk
+    const unsigned* palette;            // 256 RGBA8
+    int dims[3];
+    int cdim[3];                        // chunk counts
+    unsigned nwords;                    // number of brick words
+    unsigned ncoarse;                   // number of coarse words
+};
+
+}  // namespace vt
+
+struct vt_ctx {
+    int device = 0;
+    int sm_count = 0;
+    char name[256] = {0};
+    std::string last_error;
+    unsigned* d_status = nullptr;                // device status word
+    unsigned long long* d_counters = nullptr;    // vt::kNumCounters
+    cudaStream_t stream = nullptr;               // stream of the *_host entry points
+    void* d_scratch = nullptr;                   // output staging of the *_host entry points
+    size_t scratch_bytes = 0;
+};
+
+struct vt_world {
+    vt_ctx* ctx = nullptr;
+    int dims[3] = {0, 0, 0};
+    int cdim[3] = {0, 0, 0};
+    size_t nchunks = 0;
+    unsigned long long* d_mask = nullptr;
+    unsigned char* d_mats = nullptr;
+    unsigned long long* d_coarse = nullptr;
+    size_t ncoarse = 0;
+    unsigned* d_palette = nullptr;
+    unsigned char* d_stage = nullptr;  // upload staging (grown on demand)
+    size_t stage_bytes = 0;
+
+    vt::WorldView view() const {
+        vt::WorldView v;
+        v.mask = d_mask;
+        v.mats = d_mats;
+        v.coarse = d_coarse;
+        v.palette = d_palette;
+        for (int i = 0; i < 3; ++i) {
+            v.dims[i] = dims[i];
+            v.cdim[i] = cdim[i];
+        }
+        v.nwords = (unsigned)(nchunks * vt::kBricksPerChunk);
+        v.ncoarse = (unsigned)ncoarse;
+        return v;
+    }
+};
+
+namespace vt {
+// Records `msg` (plus the CUDA error text when err != cudaSuccess) in the
+// context and returns the matching status.
+vt_status fail(vt_ctx* ctx, vt_status s, const std::string& msg, cudaError_t err = cudaSuccess);
+vt_status check_cuda(vt_ctx* ctx, cudaError_t err, const char* what);
+// Context-owned device buffer of at least `bytes` (grown on demand).
+vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out);
+}  // namespace vt
+
+#define VT_CUDA(ctx, call)                                                      \
+    do {                                                                        \
+        cudaError_t _e = (call);                                                \
+        if (_e != cudaSuccess) return vt::check_cuda((ctx), _e, #call);         \
+    } while (0)

@@ -1,0 +1,251 @@
+// world.cu -- mode-P world storage on the device and its upload entry points.
+//
+// The reference keeps its world in two persistently mapped SSBOs that the host
+// writes voxel by voxel (VoxelBrickmap, src/engine/voxel.zig:25-82): a 64^3
+// chunk table of brick indices and a pool of 8^3 u32 bricks.  Here the host
+// hands over uint8 materials (dense, or one 32^3 chunk at a time) and a kernel
+// builds the traversal structures on the device:
+//
+//   materials  chunk-major; inside a chunk 512 bricks of 64 bytes, brick
+//              b = bx + 8*(by + 8*bz), voxel v = x + 4*(y + 4*z) in the brick
+//   mask       one u64 per brick, bit v set iff material != 0
+//   coarse     one bit per chunk, set iff any brick word of the chunk is != 0
+#include <algorithm>
+#include <cstring>
+
+#include "vt_internal.h"
+
+namespace vt {
+
+// One block per chunk, one thread per brick.  src is a dense x-fastest box of
+// sdims voxels whose voxel (0,0,0) sits at world voxel `sorg`; world cells
+// outside the source box or outside the world read as air.
+__global__ void __launch_bounds__(512) k_build_chunks(WorldView w, unsigned long long* mask, unsigned char* mats,
+                                                      unsigned long long* coarse, const unsigned char* __restrict__ src,
+                                                      int3 sdims, int3 sorg, int3 cfirst, int3 ccount) {
+    const int lin = blockIdx.x;
+    const int cx = cfirst.x + lin % ccount.x;
+    const int cy = cfirst.y + (lin / ccount.x) % ccount.y;
+    const int cz = cfirst.z + lin / (ccount.x * ccount.y);
+    const unsigned ci = (unsigned)cx + (unsigned)w.cdim[0] * ((unsigned)cy + (unsigned)w.cdim[1] * (unsigned)cz);
+    const int b = threadIdx.x;
+    const int bx = b & 7, by = (b >> 3) & 7, bz = b >> 6;
+    const unsigned wi = ci * 512u + (unsigned)b;
+    unsigned long long m = 0ull;
+    unsigned packed[16];
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+#pragma unroll
+        for (int y = 0; y < 4; ++y) {
+            unsigned word = 0;
+#pragma unroll
+            for (int x = 0; x < 4; ++x) {
+                const int gx = cx * 32 + bx * 4 + x, gy = cy * 32 + by * 4 + y, gz = cz * 32 + bz * 4 + z;
+                const int sx = gx - sorg.x, sy = gy - sorg.y, sz = gz - sorg.z;
+                unsigned v = 0;
+                if (gx < w.dims[0] && gy < w.dims[1] && gz < w.dims[2] && sx >= 0 && sy >= 0 && sz >= 0 &&
+                    sx < sdims.x && sy < sdims.y && sz < sdims.z)
+                    v = src[(size_t)sx + (size_t)sdims.x * ((size_t)sy + (size_t)sdims.y * (size_t)sz)];
+                word |= v << (8 * x);
+                if (v) m |= 1ull << (x + 4 * (y + 4 * z));
+            }
+            packed[y + 4 * z] = word;
+        }
+    }
+    uint4* dst = reinterpret_cast<uint4*>(mats + (size_t)wi * 64u);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+    mask[wi] = m;
+    const int any = __syncthreads_or(m != 0ull);
+    if (threadIdx.x == 0) {
+        const unsigned long long bit = 1ull << (ci & 63u);
+        if (any) atomicOr(coarse + (ci >> 6), bit);
+        else atomicAnd(coarse + (ci >> 6), ~bit);
+    }
+}
+
+// VoxelBrickmap.set (voxel.zig:58-61): one voxel, then the chunk's coarse bit.
+__global__ void __launch_bounds__(512) k_set_voxel(WorldView w, unsigned long long* mask, unsigned char* mats,
+                                                   unsigned long long* coarse, int x, int y, int z, unsigned mat) {
+    const unsigned ci = (unsigned)(x >> 5) + (unsigned)w.cdim[0] * ((unsigned)(y >> 5) + (unsigned)w.cdim[1] * (unsigned)(z >> 5));
+    const unsigned bi = (unsigned)((x >> 2) & 7) | ((unsigned)((y >> 2) & 7) << 3) | ((unsigned)((z >> 2) & 7) << 6);
+    const unsigned vb = (unsigned)(x & 3) | ((unsigned)(y & 3) << 2) | ((unsigned)(z & 3) << 4);
+    if (threadIdx.x == 0) {
+        const unsigned wi = ci * 512u + bi;
+        mats[(size_t)wi * 64u + vb] = (unsigned char)mat;
+        if (mat) mask[wi] |= 1ull << vb;
+        else mask[wi] &= ~(1ull << vb);
+    }
+    __syncthreads();
+    const int any = __syncthreads_or(mask[ci * 512u + threadIdx.x] != 0ull);
+    if (threadIdx.x == 0) {
+        const unsigned long long bit = 1ull << (ci & 63u);
+        if (any) atomicOr(coarse + (ci >> 6), bit);
+        else atomicAnd(coarse + (ci >> 6), ~bit);
+    }
+}
+
+static vt_status ensure_stage(vt_world* w, size_t bytes) {
+    if (bytes <= w->stage_bytes) return VT_OK;
+    if (w->d_stage) {
+        VT_CUDA(w->ctx, cudaDeviceSynchronize());
+        cudaFree(w->d_stage);
+        w->d_stage = nullptr;
+        w->stage_bytes = 0;
+    }
+    VT_CUDA(w->ctx, cudaMalloc(&w->d_stage, bytes));
+    w->stage_bytes = bytes;
+    return VT_OK;
+}
+
+static void free_world(vt_world* w) {
+    if (w->d_mask) cudaFree(w->d_mask);
+    if (w->d_mats) cudaFree(w->d_mats);
+    if (w->d_coarse) cudaFree(w->d_coarse);
+    if (w->d_palette) cudaFree(w->d_palette);
+    if (w->d_stage) cudaFree(w->d_stage);
+    delete w;
+}
+
+}  // namespace vt
+
+using namespace vt;
+
+extern "C" {
+
+vt_status vt_world_create(vt_ctx* ctx, const vt_world_desc* desc, vt_world** out) {
+    if (!ctx) return VT_ERR_ARG;
+    if (!desc || !out) return fail(ctx, VT_ERR_ARG, "null world descriptor or output");
+    *out = nullptr;
+    uint64_t cells = 1;
+    for (int i = 0; i < 3; ++i) {
+        if (desc->dims[i] < 1 || desc->dims[i] > 8192) return fail(ctx, VT_ERR_ARG, "world dims must be in [1, 8192]");
+        cells *= (uint64_t)desc->dims[i];
+    }
+    if (cells >= (1ull << 32)) return fail(ctx, VT_ERR_ARG, "world must hold fewer than 2^32 voxels");
+    vt_world* w = new (std::nothrow) vt_world();
+    if (!w) return fail(ctx, VT_ERR_OOM, "host allocation failed");
+    w->ctx = ctx;
+    for (int i = 0; i < 3; ++i) {
+        w->dims[i] = desc->dims[i];
+        w->cdim[i] = (desc->dims[i] + kChunk - 1) / kChunk;
+    }
+    w->nchunks = (size_t)w->cdim[0] * w->cdim[1] * w->cdim[2];
+    w->ncoarse = (w->nchunks + 63) / 64;
+    cudaError_t e;
+    if ((e = cudaMalloc(&w->d_mask, w->nchunks * kBricksPerChunk * 8)) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_mats, w->nchunks * (size_t)kChunkBytes)) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_coarse, w->ncoarse * 8)) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_palette, 256 * sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMemset(w->d_mask, 0, w->nchunks * kBricksPerChunk * 8)) != cudaSuccess ||
+        (e = cudaMemset(w->d_mats, 0, w->nchunks * (size_t)kChunkBytes)) != cudaSuccess ||
+        (e = cudaMemset(w->d_coarse, 0, w->ncoarse * 8)) != cudaSuccess) {
+        free_world(w);
+        return check_cuda(ctx, e, "world allocation");
+    }
+    uint32_t pal[256];
+    vt_default_palette(pal);
+    if ((e = cudaMemcpy(w->d_palette, pal, sizeof(pal), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        free_world(w);
+        return check_cuda(ctx, e, "palette upload");
+    }
+    *out = w;
+    return VT_OK;
+}
+
+vt_status vt_world_destroy(vt_world* world) {
+    if (!world) return VT_ERR_ARG;
+    cudaDeviceSynchronize();
+    free_world(world);
+    return VT_OK;
+}
+
+vt_status vt_world_clear(vt_world* w, vt_stream stream) {
+    if (!w) return VT_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    VT_CUDA(w->ctx, cudaMemsetAsync(w->d_mask, 0, w->nchunks * kBricksPerChunk * 8, s));
+    VT_CUDA(w->ctx, cudaMemsetAsync(w->d_mats, 0, w->nchunks * (size_t)kChunkBytes, s));
+    VT_CUDA(w->ctx, cudaMemsetAsync(w->d_coarse, 0, w->ncoarse * 8, s));
+    return VT_OK;
+}
+
+vt_status vt_world_upload_dense(vt_world* w, const uint8_t* h_materials, size_t nbytes, vt_stream stream) {
+    if (!w) return VT_ERR_ARG;
+    const size_t need = (size_t)w->dims[0] * w->dims[1] * w->dims[2];
+    if (!h_materials || nbytes != need) return fail(w->ctx, VT_ERR_ARG, "dense upload needs exactly X*Y*Z bytes");
+    vt_status s = ensure_stage(w, need);
+    if (s) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    VT_CUDA(w->ctx, cudaMemcpyAsync(w->d_stage, h_materials, need, cudaMemcpyHostToDevice, st));
+    const int3 sdims = make_int3(w->dims[0], w->dims[1], w->dims[2]);
+    k_build_chunks<<<(unsigned)w->nchunks, 512, 0, st>>>(w->view(), w->d_mask, w->d_mats, w->d_coarse, w->d_stage, sdims,
+                                                        make_int3(0, 0, 0), make_int3(0, 0, 0),
+                                                        make_int3(w->cdim[0], w->cdim[1], w->cdim[2]));
+    VT_CUDA(w->ctx, cudaGetLastError());
+    // the staging buffer is reused by the next upload on any stream
+    VT_CUDA(w->ctx, cudaStreamSynchronize(st));
+    return VT_OK;
+}
+
+vt_status vt_world_upload_chunk(vt_world* w, int32_t cx, int32_t cy, int32_t cz, const uint8_t* h_chunk,
+                                vt_stream stream) {
+    if (!w) return VT_ERR_ARG;
+    if (!h_chunk) return fail(w->ctx, VT_ERR_ARG, "null chunk");
+    if (cx < 0 || cy < 0 || cz < 0 || cx >= w->cdim[0] || cy >= w->cdim[1] || cz >= w->cdim[2])
+        return fail(w->ctx, VT_ERR_ARG, "chunk coordinate out of range");
+    vt_status s = ensure_stage(w, kChunkBytes);
+    if (s) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    VT_CUDA(w->ctx, cudaMemcpyAsync(w->d_stage, h_chunk, kChunkBytes, cudaMemcpyHostToDevice, st));
+    k_build_chunks<<<1, 512, 0, st>>>(w->view(), w->d_mask, w->d_mats, w->d_coarse, w->d_stage, make_int3(32, 32, 32),
+                                      make_int3(cx * 32, cy * 32, cz * 32), make_int3(cx, cy, cz), make_int3(1, 1, 1));
+    VT_CUDA(w->ctx, cudaGetLastError());
+    VT_CUDA(w->ctx, cudaStreamSynchronize(st));
+    return VT_OK;
+}
+
+vt_status vt_world_set_voxel(vt_world* w, int32_t x, int32_t y, int32_t z, uint8_t material, vt_stream stream) {
+    if (!w) return VT_ERR_ARG;
+    if (x < 0 || y < 0 || z < 0 || x >= w->dims[0] || y >= w->dims[1] || z >= w->dims[2])
+        return fail(w->ctx, VT_ERR_ARG, "voxel coordinate out of range");
+    k_set_voxel<<<1, 512, 0, (cudaStream_t)stream>>>(w->view(), w->d_mask, w->d_mats, w->d_coarse, x, y, z, material);
+    VT_CUDA(w->ctx, cudaGetLastError());
+    return VT_OK;
+}
+
+vt_status vt_world_get_voxel(vt_world* w, int32_t x, int32_t y, int32_t z, uint8_t* material) {
+    if (!w) return VT_ERR_ARG;
+    if (!material || x < 0 || y < 0 || z < 0 || x >= w->dims[0] || y >= w->dims[1] || z >= w->dims[2])
+        return fail(w->ctx, VT_ERR_ARG, "voxel coordinate out of range");
+    const unsigned ci = (unsigned)(x >> 5) + (unsigned)w->cdim[0] * ((unsigned)(y >> 5) + (unsigned)w->cdim[1] * (unsigned)(z >> 5));
+    const unsigned bi = (unsigned)((x >> 2) & 7) | ((unsigned)((y >> 2) & 7) << 3) | ((unsigned)((z >> 2) & 7) << 6);
+    const unsigned vb = (unsigned)(x & 3) | ((unsigned)(y & 3) << 2) | ((unsigned)(z & 3) << 4);
+    VT_CUDA(w->ctx, cudaDeviceSynchronize());
+    VT_CUDA(w->ctx, cudaMemcpy(material, w->d_mats + ((size_t)ci * 512u + bi) * 64u + vb, 1, cudaMemcpyDeviceToHost));
+    return VT_OK;
+}
+
+vt_status vt_world_set_palette(vt_world* w, const uint32_t* h_rgba256) {
+    if (!w) return VT_ERR_ARG;
+    if (!h_rgba256) return fail(w->ctx, VT_ERR_ARG, "null palette");
+    VT_CUDA(w->ctx, cudaMemcpy(w->d_palette, h_rgba256, 256 * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    return VT_OK;
+}
+
+vt_status vt_world_get_info(const vt_world* w, vt_world_info* info) {
+    if (!w || !info) return VT_ERR_ARG;
+    std::memset(info, 0, sizeof(*info));
+    for (int i = 0; i < 3; ++i) {
+        info->dims[i] = w->dims[i];
+        info->chunks[i] = w->cdim[i];
+    }
+    info->mask_bytes = (uint64_t)w->nchunks * kBricksPerChunk * 8;
+    info->material_bytes = (uint64_t)w->nchunks * kChunkBytes;
+    info->coarse_bytes = (uint64_t)w->ncoarse * 8;
+    info->d_mask = w->d_mask;
+    info->d_materials = w->d_mats;
+    info->d_coarse = w->d_coarse;
+    return VT_OK;
+}
+
+}  // extern "C"

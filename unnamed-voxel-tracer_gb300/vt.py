@@ -1,0 +1,397 @@
+"""Python host for libvt (include/vt.h) over ctypes.
+
+Mirrors the reference engine's render-path API so that a host written against
+the reference reads the same here:
+
+    reference (Zig)                                   here
+    VoxelBrickmap(dim, ch).init/set/get/clear          World(ctx, dims).set/get/clear/upload_dense/upload_chunk
+        src/engine/voxel.zig:25-82
+    Camera.set_pos/rotate/as_uniform_data              Camera(...).set_pos/rotate/as_uniform_data
+        src/engine/graphics/camera.zig:5-44
+    Game.render (primary + secondary + blit)           render(ctx, world, camera, params, out)
+        src/game.zig:232-256
+
+Every call goes to the CUDA library; there is no CPU path.  A missing or
+unloadable libvt.so raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "lib" / "libvt.so"
+
+# ---------------------------------------------------------------- constants
+VT_OK = 0
+STATUS_NAMES = {0: "VT_OK", 1: "VT_ERR_ARG", 2: "VT_ERR_OOM", 3: "VT_ERR_CUDA", 4: "VT_ERR_DEVICE_OOB",
+                5: "VT_ERR_TIMEOUT", 6: "VT_ERR_NO_DEVICE", 7: "VT_ERR_FORMAT", 8: "VT_ERR_STATE"}
+RAYS_PRIMARY, RAYS_SHADOW, RAYS_BOUNCE = 1, 2, 4
+SHADE_NONE, SHADE_REFERENCE, SHADE_LAMBERT = 0, 1, 2
+FLAG_CROSSHAIR, FLAG_VIGNETTE, FLAG_CHECKED = 1, 2, 4
+HIT_PRIMARY, HIT_SHADOWED, HIT_BOUNCE = 1, 2, 4
+
+
+class Camera_t(C.Structure):
+    _fields_ = [("pos", C.c_float * 4), ("view", C.c_float * 16), ("fov", C.c_float),
+                ("tan_half_fov", C.c_float), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class Params_t(C.Structure):
+    _fields_ = [("max_steps", C.c_int32), ("shadow_max_steps", C.c_int32), ("bounce_max_steps", C.c_int32),
+                ("rays", C.c_uint32), ("shade", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint32),
+                ("sun_dir", C.c_float * 3), ("ambient", C.c_float), ("diffuse", C.c_float),
+                ("bounce_weight", C.c_float)]
+
+
+class Stats_t(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "primary_rays", "primary_hits", "shadow_rays", "shadow_hits", "bounce_rays", "bounce_hits",
+        "mask_words", "coarse_words", "material_bytes", "record_bytes", "steps", "iterations")]
+
+    def as_dict(self) -> dict:
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+class WorldDesc_t(C.Structure):
+    _fields_ = [("dims", C.c_int32 * 3)]
+
+
+class WorldInfo_t(C.Structure):
+    _fields_ = [("dims", C.c_int32 * 3), ("chunks", C.c_int32 * 3), ("mask_bytes", C.c_uint64),
+                ("material_bytes", C.c_uint64), ("coarse_bytes", C.c_uint64), ("d_mask", C.c_void_p),
+                ("d_materials", C.c_void_p), ("d_coarse", C.c_void_p)]
+
+
+class GenDesc_t(C.Structure):
+    _fields_ = [("dims", C.c_int32 * 3), ("base_height", C.c_float), ("amplitude", C.c_float),
+                ("period", C.c_float), ("water_level", C.c_float), ("camera_height", C.c_float),
+                ("octaves", C.c_int32), ("trees", C.c_int32), ("caves", C.c_int32),
+                ("cave_threshold", C.c_float), ("cave_period", C.c_float), ("seed", C.c_uint64)]
+
+
+# numpy view of vt_hit (16 bytes)
+HIT_DTYPE = np.dtype([("voxel", "<u4"), ("t", "<f4"), ("rgba", "<u4"), ("face", "u1"), ("material", "u1"),
+                      ("flags", "u1"), ("pad", "u1")])
+assert HIT_DTYPE.itemsize == 16
+
+_P = C.c_void_p
+_S = C.c_int32
+_SIGNATURES = {
+    "vt_abi_version": (C.c_int32, []),
+    "vt_status_string": (C.c_char_p, [_S]),
+    "vt_ctx_create": (_S, [C.c_int32, C.POINTER(_P)]),
+    "vt_ctx_destroy": (_S, [_P]),
+    "vt_last_error_string": (C.c_char_p, [_P]),
+    "vt_sync": (_S, [_P, _P]),
+    "vt_device_info": (_S, [_P, C.c_char_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "vt_device_alloc": (_S, [_P, C.c_size_t, C.POINTER(_P)]),
+    "vt_device_free": (_S, [_P, _P]),
+    "vt_host_alloc_pinned": (_S, [_P, C.c_size_t, C.POINTER(_P)]),
+    "vt_host_free_pinned": (_S, [_P, _P]),
+    "vt_memcpy_h2d": (_S, [_P, _P, _P, C.c_size_t, _P]),
+    "vt_memcpy_d2h": (_S, [_P, _P, _P, C.c_size_t, _P]),
+    "vt_memset_d": (_S, [_P, _P, C.c_int32, C.c_size_t, _P]),
+    "vt_stream_create": (_S, [_P, C.POINTER(_P)]),
+    "vt_stream_destroy": (_S, [_P, _P]),
+    "vt_world_create": (_S, [_P, C.POINTER(WorldDesc_t), C.POINTER(_P)]),
+    "vt_world_destroy": (_S, [_P]),
+    "vt_world_clear": (_S, [_P, _P]),
+    "vt_world_upload_dense": (_S, [_P, _P, C.c_size_t, _P]),
+    "vt_world_upload_chunk": (_S, [_P, C.c_int32, C.c_int32, C.c_int32, _P, _P]),
+    "vt_world_set_voxel": (_S, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_uint8, _P]),
+    "vt_world_get_voxel": (_S, [_P, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_uint8)]),
+    "vt_world_set_palette": (_S, [_P, _P]),
+    "vt_world_get_info": (_S, [_P, C.POINTER(WorldInfo_t)]),
+    "vt_camera_look": (_S, [C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float, C.c_int32, C.c_int32,
+                            C.POINTER(Camera_t)]),
+    "vt_params_default": (None, [C.POINTER(Params_t)]),
+    "vt_render": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), _P, _P]),
+    "vt_render_host": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), _P]),
+    "vt_render_stats": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), C.POINTER(Stats_t), _P]),
+    "vt_trace_rays": (_S, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, _P]),
+    "vt_gen_desc_init": (None, [C.POINTER(GenDesc_t), C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64]),
+    "vt_gen_world": (_S, [C.POINTER(GenDesc_t), _P, C.c_size_t, C.c_int32]),
+    "vt_gen_height": (C.c_int32, [C.POINTER(GenDesc_t), C.c_int32, C.c_int32]),
+    "vt_gen_camera": (_S, [C.POINTER(GenDesc_t), C.c_uint64, C.c_int32, C.c_int32, C.POINTER(Camera_t)]),
+    "vt_default_palette": (_S, [_P]),
+    "vt_gen_sun": (_S, [C.c_uint64, C.POINTER(C.c_float)]),
+}
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Loads libvt.so; raises if it is missing (no fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"libvt.so not found at {p}: build it with __graft_entry__.build() "
+                           f"(python unnamed-voxel-tracer_gb300/build.py)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class VTError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def _check(status: int, ctx=None) -> None:
+    if status != VT_OK:
+        lib = load()
+        msg = lib.vt_last_error_string(ctx).decode() if ctx else lib.vt_status_string(status).decode()
+        raise VTError(status, msg)
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+# ------------------------------------------------------------------ context
+class Context:
+    """One CUDA device; owns the library context (vt_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.vt_ctx_create(device, C.byref(h))
+        if st != VT_OK:
+            raise VTError(st, self.lib.vt_status_string(st).decode())
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.vt_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def check(self, st: int) -> None:
+        _check(st, self.handle)
+
+    def sync(self, stream=None) -> None:
+        self.check(self.lib.vt_sync(self.handle, stream))
+
+    def device_info(self) -> tuple[str, int]:
+        buf = C.create_string_buffer(256)
+        sms = C.c_int32()
+        self.check(self.lib.vt_device_info(self.handle, buf, 256, C.byref(sms)))
+        return buf.value.decode(), sms.value
+
+    # device memory helpers
+    def alloc(self, nbytes: int) -> "DeviceBuffer":
+        return DeviceBuffer(self, nbytes)
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self.check(self.lib.vt_stream_create(self.handle, C.byref(s)))
+        return s.value
+
+
+class DeviceBuffer:
+    def __init__(self, ctx: Context, nbytes: int):
+        self.ctx, self.nbytes = ctx, int(nbytes)
+        p = C.c_void_p()
+        ctx.check(ctx.lib.vt_device_alloc(ctx.handle, self.nbytes, C.byref(p)))
+        self.ptr = p.value
+
+    def upload(self, a: np.ndarray, stream=None) -> None:
+        a = np.ascontiguousarray(a)
+        assert a.nbytes <= self.nbytes
+        self.ctx.check(self.ctx.lib.vt_memcpy_h2d(self.ctx.handle, self.ptr, _ptr(a), a.nbytes, stream))
+        self.ctx.sync(stream)
+
+    def download(self, out: np.ndarray, stream=None) -> np.ndarray:
+        assert out.flags.c_contiguous and out.nbytes <= self.nbytes
+        self.ctx.check(self.ctx.lib.vt_memcpy_d2h(self.ctx.handle, _ptr(out), self.ptr, out.nbytes, stream))
+        self.ctx.sync(stream)
+        return out
+
+    def zero(self, stream=None) -> None:
+        self.ctx.check(self.ctx.lib.vt_memset_d(self.ctx.handle, self.ptr, 0, self.nbytes, stream))
+
+    def free(self) -> None:
+        if self.ptr:
+            self.ctx.lib.vt_device_free(self.ctx.handle, self.ptr)
+            self.ptr = None
+
+
+# -------------------------------------------------------------------- world
+class World:
+    """Mode-P voxel world on the device (VoxelBrickmap, voxel.zig:25-82)."""
+
+    def __init__(self, ctx: Context, dims):
+        self.ctx = ctx
+        self.dims = tuple(int(d) for d in dims)
+        desc = WorldDesc_t((C.c_int32 * 3)(*self.dims))
+        h = C.c_void_p()
+        ctx.check(ctx.lib.vt_world_create(ctx.handle, C.byref(desc), C.byref(h)))
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.vt_world_destroy(self.handle)
+            self.handle = None
+
+    def upload_dense(self, mats: np.ndarray, stream=None) -> None:
+        """mats: uint8 array indexed [z, y, x] (x fastest), shape (Z, Y, X)."""
+        X, Y, Z = self.dims
+        mats = np.ascontiguousarray(mats, dtype=np.uint8)
+        if mats.shape != (Z, Y, X):
+            raise ValueError(f"expected shape {(Z, Y, X)}, got {mats.shape}")
+        self.ctx.check(self.ctx.lib.vt_world_upload_dense(self.handle, _ptr(mats), mats.nbytes, stream))
+
+    def upload_chunk(self, cx: int, cy: int, cz: int, chunk: np.ndarray, stream=None) -> None:
+        chunk = np.ascontiguousarray(chunk, dtype=np.uint8)
+        if chunk.size != 32 ** 3:
+            raise ValueError("a chunk is 32^3 bytes")
+        self.ctx.check(self.ctx.lib.vt_world_upload_chunk(self.handle, cx, cy, cz, _ptr(chunk), stream))
+
+    def set(self, x: int, y: int, z: int, material: int, stream=None) -> None:
+        self.ctx.check(self.ctx.lib.vt_world_set_voxel(self.handle, x, y, z, material, stream))
+
+    def get(self, x: int, y: int, z: int) -> int:
+        m = C.c_uint8()
+        self.ctx.check(self.ctx.lib.vt_world_get_voxel(self.handle, x, y, z, C.byref(m)))
+        return int(m.value)
+
+    def clear(self, stream=None) -> None:
+        self.ctx.check(self.ctx.lib.vt_world_clear(self.handle, stream))
+
+    def set_palette(self, rgba: np.ndarray) -> None:
+        rgba = np.ascontiguousarray(rgba, dtype=np.uint32)
+        assert rgba.size == 256
+        self.ctx.check(self.ctx.lib.vt_world_set_palette(self.handle, _ptr(rgba)))
+
+    def info(self) -> WorldInfo_t:
+        info = WorldInfo_t()
+        self.ctx.check(self.ctx.lib.vt_world_get_info(self.handle, C.byref(info)))
+        return info
+
+
+# ------------------------------------------------------------------- camera
+class Camera:
+    """Camera.set_pos / rotate / as_uniform_data (camera.zig:5-44).
+
+    yaw and pitch in radians; a negative pitch looks down.  rotate() applies
+    mouse deltas with the reference's 0.001 gain and pitch clamp.
+    """
+
+    def __init__(self, pos=(0.0, 0.0, 0.0), yaw=0.0, pitch=0.0, fov=math.pi / 2, width=1280, height=720):
+        self.pos = [float(p) for p in pos]
+        self.yaw, self.pitch, self.fov = float(yaw), float(pitch), float(fov)
+        self.width, self.height = int(width), int(height)
+
+    def set_pos(self, pos) -> None:
+        self.pos = [float(p) for p in pos]
+
+    def rotate(self, pitch_delta: float, yaw_delta: float) -> None:
+        self.pitch = min(max(self.pitch + pitch_delta * 0.001, -math.pi / 2), math.pi / 2)
+        self.yaw = self.yaw + yaw_delta * 0.001
+
+    def as_uniform_data(self) -> Camera_t:
+        lib = load()
+        cam = Camera_t()
+        pos = (C.c_float * 3)(*self.pos)
+        _check(lib.vt_camera_look(pos, self.yaw, self.pitch, self.fov, self.width, self.height, C.byref(cam)))
+        return cam
+
+
+def default_params(**kw) -> Params_t:
+    p = Params_t()
+    load().vt_params_default(C.byref(p))
+    for k, v in kw.items():
+        if k == "sun_dir":
+            p.sun_dir = (C.c_float * 3)(*v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def render(ctx: Context, world: World, cam: Camera_t, params: Params_t, d_out: DeviceBuffer, stream=None) -> None:
+    """Game.render: one fused launch writing width*height vt_hit records."""
+    assert d_out.nbytes >= cam.width * cam.height * 16
+    ctx.check(ctx.lib.vt_render(ctx.handle, world.handle, C.byref(cam), C.byref(params), d_out.ptr, stream))
+
+
+def render_host(ctx: Context, world: World, cam: Camera_t, params: Params_t, out: np.ndarray | None = None):
+    if out is None:
+        out = np.zeros(cam.width * cam.height, dtype=HIT_DTYPE)
+    assert out.dtype == HIT_DTYPE and out.size >= cam.width * cam.height
+    ctx.check(ctx.lib.vt_render_host(ctx.handle, world.handle, C.byref(cam), C.byref(params), _ptr(out)))
+    return out
+
+
+def render_stats(ctx: Context, world: World, cam: Camera_t, params: Params_t, stream=None) -> dict:
+    st = Stats_t()
+    ctx.check(ctx.lib.vt_render_stats(ctx.handle, world.handle, C.byref(cam), C.byref(params), C.byref(st), stream))
+    return st.as_dict()
+
+
+def trace_rays(ctx: Context, world: World, origins: np.ndarray, dirs: np.ndarray, max_steps: int) -> np.ndarray:
+    origins = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)
+    dirs = np.ascontiguousarray(dirs, dtype=np.float32).reshape(-1, 3)
+    n = origins.shape[0]
+    do, dd, dh = ctx.alloc(origins.nbytes), ctx.alloc(dirs.nbytes), ctx.alloc(max(n, 1) * 16)
+    try:
+        do.upload(origins)
+        dd.upload(dirs)
+        ctx.check(ctx.lib.vt_trace_rays(ctx.handle, world.handle, do.ptr, dd.ptr, n, max_steps, dh.ptr, None))
+        ctx.sync()
+        out = np.zeros(n, dtype=HIT_DTYPE)
+        if n:
+            dh.download(out)
+        return out
+    finally:
+        do.free(), dd.free(), dh.free()
+
+
+# --------------------------------------------------------------- generators
+def gen_desc(dims, scale: float = 1.0, seed: int = 0, trees: int = 0, caves: bool = False) -> GenDesc_t:
+    d = GenDesc_t()
+    load().vt_gen_desc_init(C.byref(d), int(dims[0]), int(dims[1]), int(dims[2]), float(scale), int(seed))
+    d.trees = int(trees)
+    d.caves = 1 if caves else 0
+    return d
+
+
+def gen_world(desc: GenDesc_t, threads: int = 0) -> np.ndarray:
+    X, Y, Z = desc.dims
+    out = np.zeros((Z, Y, X), dtype=np.uint8)
+    _check(load().vt_gen_world(C.byref(desc), _ptr(out), out.nbytes, threads))
+    return out
+
+
+def gen_camera(desc: GenDesc_t, seed: int, width: int, height: int) -> Camera_t:
+    cam = Camera_t()
+    _check(load().vt_gen_camera(C.byref(desc), int(seed), int(width), int(height), C.byref(cam)))
+    return cam
+
+
+def gen_sun(seed: int):
+    out = (C.c_float * 3)()
+    _check(load().vt_gen_sun(int(seed), out))
+    return [float(v) for v in out]
+
+
+def default_palette() -> np.ndarray:
+    pal = np.zeros(256, dtype=np.uint32)
+    _check(load().vt_default_palette(_ptr(pal)))
+    return pal
