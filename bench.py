@@ -305,6 +305,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2,
                         "peak_kind": "24 MiB device copy held in L2, read+write bytes, this run"},
         "rays_per_step": total_rays / args.steps,
+        "per_ray": {k: sum(s[k] for s in stats) / sum(rays) for k in ("steps", "iterations", "mask_words",
+                                                                       "coarse_words")},
         "e2e": {"value": e2e_value, "unit": "Grays/s", "h2d_bytes_per_step": C.sizeof(vt.Camera_t) + C.sizeof(vt.Params_t),
                 "d2h_bytes_per_step": nbytes,
                 "note": "vt_render_host: camera and params travel in the launch; records copied to pinned host memory"},
@@ -318,8 +320,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

@@ -541,7 +541,7 @@ void vto_trace_rays(const vto_world* w, const float* origins, const float* dirs,
         h.face = tr.hit ? (uint8_t)tr.face : 0xFF;
         h.material = tr.material;
         h.flags = tr.hit ? VT_HIT_PRIMARY : 0;
-        h.rgba = tr.hit ? (uint32_t)tr.steps : 0u;
+        h.rgba = 0u;
         out[i] = h;
     }
 }

@@ -27,9 +27,32 @@ static inline unsigned atomicOr(unsigned* p, unsigned v) { unsigned o = *p; *p |
 
 #include "../../unnamed-voxel-tracer_gb300/csrc/trace_p.cuh"
 
+// Chebyshev distance (capped at kDistCap + 1) from each cell of a gx*gy*gz
+// occupancy grid to the nearest occupied cell, by brute force over the window.
+static std::vector<unsigned char> cheb(const std::vector<unsigned char>& occ, int gx, int gy, int gz) {
+    const int cap = vt::kDistCap;
+    std::vector<unsigned char> d((size_t)gx * gy * gz);
+    for (int z = 0; z < gz; ++z)
+        for (int y = 0; y < gy; ++y)
+            for (int x = 0; x < gx; ++x) {
+                int best = cap + 1;
+                for (int r = 0; r <= cap && best > cap; ++r)
+                    for (int dz = -r; dz <= r && best > cap; ++dz)
+                        for (int dy = -r; dy <= r && best > cap; ++dy)
+                            for (int dx = -r; dx <= r; ++dx) {
+                                if (std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz))) != r) continue;
+                                int qx = x + dx, qy = y + dy, qz = z + dz;
+                                if (qx < 0 || qy < 0 || qz < 0 || qx >= gx || qy >= gy || qz >= gz) continue;
+                                if (occ[(size_t)qx + (size_t)gx * ((size_t)qy + (size_t)gy * qz)]) { best = r; break; }
+                            }
+                d[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] = (unsigned char)best;
+            }
+    return d;
+}
+
 extern "C" int ht_trace_rays(const int32_t dims[3], const uint8_t* dense, const float* origins, const float* dirs,
                              int32_t n, int32_t max_steps, uint32_t* out /* n * 4 u32, vt_hit layout */,
-                             uint64_t* counters /* mask, coarse */) {
+                             uint64_t* counters /* mask, coarse */, int32_t fast) {
     vt::WorldView w;
     int cd[3];
     for (int i = 0; i < 3; ++i) {
@@ -57,20 +80,44 @@ extern "C" int ht_trace_rays(const int32_t dims[3], const uint8_t* dense, const 
     w.palette = nullptr;
     w.nwords = (unsigned)(nch * 512);
     w.ncoarse = (unsigned)coarse.size();
+    // empty-space distances in the kernel's brick order and chunk order
+    const int gx = cd[0] * 8, gy = cd[1] * 8, gz = cd[2] * 8;
+    std::vector<unsigned char> bocc((size_t)gx * gy * gz), cocc(nch);
+    for (int z = 0; z < gz; ++z)
+        for (int y = 0; y < gy; ++y)
+            for (int x = 0; x < gx; ++x) {
+                size_t ci = (size_t)(x >> 3) + cd[0] * ((size_t)(y >> 3) + (size_t)cd[1] * (z >> 3));
+                unsigned bi = (x & 7) | ((y & 7) << 3) | ((z & 7) << 6);
+                bocc[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] = mask[ci * 512 + bi] != 0;
+                if (mask[ci * 512 + bi]) cocc[ci] = 1;
+            }
+    std::vector<unsigned char> bd = cheb(bocc, gx, gy, gz), cdd = cheb(cocc, cd[0], cd[1], cd[2]);
+    std::vector<unsigned char> bdist(nch * 512);
+    for (int z = 0; z < gz; ++z)
+        for (int y = 0; y < gy; ++y)
+            for (int x = 0; x < gx; ++x) {
+                size_t ci = (size_t)(x >> 3) + cd[0] * ((size_t)(y >> 3) + (size_t)cd[1] * (z >> 3));
+                unsigned bi = (x & 7) | ((y & 7) << 3) | ((z & 7) << 6);
+                bdist[ci * 512 + bi] = bd[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)];
+            }
+    w.bdist = bdist.data();
+    w.cdist = cdd.data();
+    w.nchunks = (unsigned)nch;
     unsigned status = 0;
     for (int i = 0; i < n; ++i) {
         vt::PRay r;
         vt::pray_init(r, origins + 3 * i, dirs + 3 * i);
         vt::TraceHit h;
         vt::TraceCounters cnt;
-        bool hit = vt::trace_p<true, true, true>(w, vt::CoarseGlobal{w.coarse}, r, max_steps, h, cnt, &status);
+        bool hit = fast ? vt::trace_fast<true>(w, w.cdist, r, max_steps, h)
+                        : vt::trace_p<true, true, true>(w, vt::CoarseGlobal{w.coarse}, r, max_steps, h, cnt, &status);
         uint32_t* o = out + 4 * i;
         if (hit) {
             const int e = h.axis;
             const bool pe = r.pos[e];
             o[0] = (uint32_t)h.c[0] + (uint32_t)dims[0] * ((uint32_t)h.c[1] + (uint32_t)dims[1] * (uint32_t)h.c[2]);
             memcpy(&o[1], &h.t, 4);
-            o[2] = cnt.steps;
+            o[2] = fast ? 0u : cnt.steps;
             o[3] = (2u * e + (pe ? 0u : 1u)) | (h.mat << 8) | (1u << 16);
         } else {
             float mt = -1.0f;

@@ -19,8 +19,8 @@ def compare(gpu, ref, rgb_tol=RGB_TOL):
         assert bad.size == 0, f"{f}: {bad.size} mismatches, first at {bad[:5]}: gpu {gpu[bad[:5]]} ref {ref[bad[:5]]}"
     bad = np.flatnonzero(gpu["t"].view(np.uint32) != ref["t"].view(np.uint32))
     assert bad.size == 0, f"t: {bad.size} mismatches, first {gpu['t'][bad[:5]]} vs {ref['t'][bad[:5]]}"
-    g = gpu["rgba"].view(np.uint8).reshape(-1, 4).astype(np.int16)
-    r = ref["rgba"].view(np.uint8).reshape(-1, 4).astype(np.int16)
+    g = np.ascontiguousarray(gpu["rgba"]).view(np.uint8).reshape(-1, 4).astype(np.int16)
+    r = np.ascontiguousarray(ref["rgba"]).view(np.uint8).reshape(-1, 4).astype(np.int16)
     assert np.abs(g - r).max(initial=0) <= rgb_tol
 
 

@@ -35,17 +35,17 @@ def ht():
     lib = C.CDLL(str(OUT))
     lib.ht_trace_rays.restype = C.c_int
     P = C.c_void_p
-    lib.ht_trace_rays.argtypes = [C.POINTER(C.c_int32), P, P, P, C.c_int32, C.c_int32, P, P]
+    lib.ht_trace_rays.argtypes = [C.POINTER(C.c_int32), P, P, P, C.c_int32, C.c_int32, P, P, C.c_int32]
     return lib
 
 
-def run_host(ht, mats, o, d, steps):
+def run_host(ht, mats, o, d, steps, fast=0):
     Z, Y, X = mats.shape
     n = o.shape[0]
     out = np.zeros(n * 4, dtype=np.uint32)
     cnt = np.zeros(2, dtype=np.uint64)
     st = ht.ht_trace_rays((C.c_int32 * 3)(X, Y, Z), mats.ctypes.data, o.ctypes.data, d.ctypes.data, n, steps,
-                          out.ctypes.data, cnt.ctypes.data)
+                          out.ctypes.data, cnt.ctypes.data, fast)
     assert st == 0, "bounds check fired"
     return out.view(np.dtype([("voxel", "<u4"), ("t", "<f4"), ("rgba", "<u4"), ("face", "u1"),
                               ("material", "u1"), ("flags", "u1"), ("pad", "u1")])), cnt
@@ -65,9 +65,14 @@ def random_rays(rng, dims, n):
 
 
 def check(ht, oracle, mats, o, d, steps):
-    got, _ = run_host(ht, mats, o, d, steps)
     ref = oracle.trace_rays(oracle.OracleWorld(mats), o, d, steps)
-    for f in ("voxel", "face", "material", "flags", "rgba"):
+    for fast in (0, 1):
+        got, _ = run_host(ht, mats, o, d, steps, fast)
+        compare_exact(got, ref, o, d, fields=("voxel", "face", "material", "flags"))
+
+
+def compare_exact(got, ref, o, d, fields):
+    for f in fields:
         bad = np.flatnonzero(got[f] != ref[f])
         assert bad.size == 0, (f, bad[:5], o[bad[:3]], d[bad[:3]], got[bad[:3]], ref[bad[:3]])
     assert np.array_equal(got["t"].view(np.uint32), ref["t"].view(np.uint32))

@@ -84,7 +84,8 @@ vt_status vt_ctx_create(int32_t device, vt_ctx** out) {
         if ((e = cudaMalloc(&ctx->d_status, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
         if ((e = cudaMemset(ctx->d_status, 0, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMemset"); break; }
         if ((e = cudaMalloc(&ctx->d_counters, kNumCounters * sizeof(unsigned long long))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
-        if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaStreamCreate"); break; }
+        // blocking stream: *_host calls order after work queued on the legacy default stream
+        if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamDefault)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaStreamCreate"); break; }
     } while (0);
     if (s != VT_OK) {
         vt_ctx_destroy(ctx);

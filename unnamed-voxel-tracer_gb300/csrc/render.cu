@@ -26,16 +26,28 @@ struct PixelCounters {
     unsigned v[kNumCounters];
 };
 
+// The instrumented and bounds-checked variants run the three-level model
+// traversal (it defines the algorithmic byte counts); the production variant
+// runs trace_fast.  Both give identical results.
+template <bool STATS, bool CHECKED, bool MAT, class Coarse>
+__device__ __forceinline__ bool trace_any(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
+                                          const PRay& r, int max_steps, TraceHit& h, TraceCounters& cnt,
+                                          unsigned* status) {
+    if (STATS || CHECKED) return trace_p<STATS, CHECKED, MAT>(w, coarse, r, max_steps, h, cnt, status);
+    return trace_fast<MAT>(w, cd, r, max_steps, h);
+}
+
 template <bool STATS, bool CHECKED, class Coarse>
-__device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& coarse, const FrameParams& f, int px,
-                                              int py, unsigned* status, PixelCounters& pc) {
+__device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
+                                              const FrameParams& f, int px, int py, unsigned* status,
+                                              PixelCounters& pc) {
     float o[3], d[3];
     primary_ray(f, px, py, o, d);
     PRay r;
     pray_init(r, o, d);
     TraceHit h;
     TraceCounters cnt;
-    const bool hit = trace_p<STATS, CHECKED, true>(w, coarse, r, f.max_steps, h, cnt, status);
+    const bool hit = trace_any<STATS, CHECKED, true>(w, coarse, cd, r, f.max_steps, h, cnt, status);
     if (STATS) {
         pc.v[0] += 1;
         pc.v[9] += 16;
@@ -68,7 +80,7 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
             PRay rs;
             pray_init(rs, so, f.sun);
             TraceHit hs;
-            shadowed = trace_p<STATS, CHECKED, false>(w, coarse, rs, f.shadow_max_steps, hs, cnt, status);
+            shadowed = trace_any<STATS, CHECKED, false>(w, coarse, cd, rs, f.shadow_max_steps, hs, cnt, status);
             if (shadowed) flags |= VT_HIT_SHADOWED;
             if (STATS) {
                 pc.v[2] += 1;
@@ -83,7 +95,7 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
             PRay rb;
             pray_init(rb, so, bdir);
             TraceHit hb;
-            const bool bh = trace_p<STATS, CHECKED, false>(w, coarse, rb, f.bounce_max_steps, hb, cnt, status);
+            const bool bh = trace_any<STATS, CHECKED, false>(w, coarse, cd, rb, f.bounce_max_steps, hb, cnt, status);
             if (bh) flags |= VT_HIT_BOUNCE;
             bounce_open = !bh;
             if (STATS) {
@@ -119,9 +131,18 @@ __device__ __forceinline__ void flush_counters(PixelCounters& pc, unsigned long 
 template <bool STATS, bool CHECKED, bool SMEM>
 __global__ void __launch_bounds__(kBlock) k_render(WorldView w, FrameParams f, uint4* __restrict__ out,
                                                    unsigned* status, unsigned long long* counters) {
-    extern __shared__ unsigned long long s_coarse[];
+    // shared copy of the coarse level: per-chunk distances (production) or
+    // coarse bits (model traversal)
+    extern __shared__ uint4 s_dyn[];
+    unsigned long long* s_coarse = reinterpret_cast<unsigned long long*>(s_dyn);
+    unsigned char* s_cdist = reinterpret_cast<unsigned char*>(s_dyn);
     if (SMEM) {
-        for (unsigned i = threadIdx.x; i < w.ncoarse; i += blockDim.x) s_coarse[i] = __ldg(w.coarse + i);
+        if (STATS || CHECKED) {
+            for (unsigned i = threadIdx.x; i < w.ncoarse; i += blockDim.x) s_coarse[i] = __ldg(w.coarse + i);
+        } else {
+            const uint4* src = reinterpret_cast<const uint4*>(w.cdist);
+            for (unsigned i = threadIdx.x; i < (w.nchunks + 15u) / 16u; i += blockDim.x) s_dyn[i] = __ldg(src + i);
+        }
         __syncthreads();
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -132,14 +153,14 @@ __global__ void __launch_bounds__(kBlock) k_render(WorldView w, FrameParams f, u
     for (int k = 0; k < kNumCounters; ++k) pc.v[k] = 0;
     if (px < f.width && py < f.height) {
         uint4 rec;
-        if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, f, px, py, status, pc);
-        else rec = render_pixel<STATS, CHECKED>(w, CoarseGlobal{w.coarse}, f, px, py, status, pc);
+        if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, s_cdist, f, px, py, status, pc);
+        else rec = render_pixel<STATS, CHECKED>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, status, pc);
         out[(size_t)py * f.width + px] = rec;
     }
     flush_counters<STATS>(pc, counters);
 }
 
-// Explicit ray list: record.rgba carries the crossing count on a hit.
+// Explicit ray list (production traversal); record.rgba is 0.
 template <bool CHECKED>
 __global__ void __launch_bounds__(kBlock) k_trace_rays(WorldView w, const float* __restrict__ origins,
                                                        const float* __restrict__ dirs, int n, int max_steps,
@@ -156,13 +177,13 @@ __global__ void __launch_bounds__(kBlock) k_trace_rays(WorldView w, const float*
     pray_init(r, o, d);
     TraceHit h;
     TraceCounters cnt;
-    const bool hit = trace_p<true, CHECKED, true>(w, CoarseGlobal{w.coarse}, r, max_steps, h, cnt, status);
+    const bool hit = trace_fast<true>(w, w.cdist, r, max_steps, h);
     if (hit) {
         const int e = h.axis;
         const bool pe = e == 0 ? r.pos[0] : (e == 1 ? r.pos[1] : r.pos[2]);
         const unsigned voxel = (unsigned)h.c[0] + (unsigned)w.dims[0] * ((unsigned)h.c[1] + (unsigned)w.dims[1] * (unsigned)h.c[2]);
         const unsigned face = 2u * (unsigned)e + (pe ? 0u : 1u);
-        out[i] = make_uint4(voxel, __float_as_uint(h.t), cnt.steps, face | (h.mat << 8) | (VT_HIT_PRIMARY << 16));
+        out[i] = make_uint4(voxel, __float_as_uint(h.t), 0u, face | (h.mat << 8) | (VT_HIT_PRIMARY << 16));
     } else {
         out[i] = make_uint4(0xFFFFFFFFu, __float_as_uint(-1.0f), 0u, 0xFFu);
     }
@@ -188,6 +209,7 @@ FrameParams make_frame(const vt_camera* cam, const vt_params* p) {
     f.ambient = p->ambient;
     f.diffuse = p->diffuse;
     f.bounce_weight = p->bounce_weight;
+    frame_constants(f);
     return f;
 }
 
@@ -206,9 +228,14 @@ static vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_came
     const FrameParams f = make_frame(cam, p);
     const WorldView w = world->view();
     const dim3 grid((cam->width + kTileW - 1) / kTileW, (cam->height + kTileH - 1) / kTileH);
-    const size_t smem = (size_t)w.ncoarse * sizeof(unsigned long long);
-    const bool use_smem = smem <= kMaxSharedCoarse;
     const bool checked = (p->flags & VT_FLAG_CHECKED) != 0;
+    const size_t smem = (stats || checked) ? (size_t)w.ncoarse * sizeof(unsigned long long)
+                                           : (size_t)((w.nchunks + 15u) / 16u) * 16u;
+    const bool use_smem = smem <= kMaxSharedCoarse;
+    if (world->dist_dirty) {
+        vt_status s = rebuild_distances(const_cast<vt_world*>(world), stream);
+        if (s) return s;
+    }
     const size_t sm = use_smem ? smem : 0;
 #define VT_LAUNCH(S, C, M) k_render<S, C, M><<<grid, kBlock, sm, stream>>>(w, f, d_out, ctx->d_status, ctx->d_counters)
     if (stats) {
@@ -301,6 +328,10 @@ vt_status vt_trace_rays(vt_ctx* ctx, const vt_world* world, const float* d_origi
     if (!ctx) return VT_ERR_ARG;
     if (!world || !d_origins || !d_dirs || !d_out || n < 0) return fail(ctx, VT_ERR_ARG, "bad trace_rays arguments");
     if (n == 0) return VT_OK;
+    if (world->dist_dirty) {
+        vt_status s = rebuild_distances(const_cast<vt_world*>(world), (cudaStream_t)stream);
+        if (s) return s;
+    }
     const WorldView w = world->view();
     k_trace_rays<true><<<(n + kBlock - 1) / kBlock, kBlock, 0, (cudaStream_t)stream>>>(
         w, d_origins, d_dirs, n, max_steps, reinterpret_cast<uint4*>(d_out), ctx->d_status);

@@ -26,6 +26,10 @@ struct FrameParams {
     unsigned rays, shade, flags, seed;
     float sun[3];
     float ambient, diffuse, bounce_weight;
+    // per-frame constants, computed on the host by the same code as the device
+    float sun_n[3];     // normalised sun direction
+    float lit_sky[3];   // SkyDome2 of the RGBA8-stored sun direction (blit.fragment.glsl:31)
+    float lit_a;        // illumination alpha 0.3 stored in RGBA8
 };
 
 __device__ __forceinline__ void primary_ray(const FrameParams& f, int px, int py, float o[3], float d[3]) {
@@ -46,20 +50,22 @@ __device__ __forceinline__ void primary_ray(const FrameParams& f, int px, int py
     }
 }
 
-__device__ __forceinline__ float clampf(float x, float a, float b) { return x < a ? a : (x > b ? b : x); }
+// Shared by host and device: plain IEEE operators (correctly rounded division
+// and square root on both sides, no contraction).
+__host__ __device__ __forceinline__ float clampf(float x, float a, float b) { return x < a ? a : (x > b ? b : x); }
 
-__device__ __forceinline__ unsigned unorm8(float x) { return (unsigned)__float2int_rn(clampf(x, 0.0f, 1.0f) * 255.0f); }
+__host__ __device__ __forceinline__ unsigned unorm8(float x) { return (unsigned)(int)rintf(clampf(x, 0.0f, 1.0f) * 255.0f); }
 
-__device__ __forceinline__ float dot3(const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+__host__ __device__ __forceinline__ float dot3(const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
 
-__device__ __forceinline__ void normalize3(const float a[3], float o[3]) {
-    const float len = __fsqrt_rn(dot3(a, a));
-    o[0] = __fdiv_rn(a[0], len);
-    o[1] = __fdiv_rn(a[1], len);
-    o[2] = __fdiv_rn(a[2], len);
+__host__ __device__ __forceinline__ void normalize3(const float a[3], float o[3]) {
+    const float len = sqrtf(dot3(a, a));
+    o[0] = a[0] / len;
+    o[1] = a[1] / len;
+    o[2] = a[2] / len;
 }
 
-__device__ __forceinline__ void sky(const float sun[3], const float rd[3], float col[3]) {
+__host__ __device__ __forceinline__ void sky(const float sun[3], const float rd[3], float col[3]) {
     float sn[3], rn[3];
     normalize3(sun, sn);
     normalize3(rd, rn);
@@ -153,13 +159,9 @@ __device__ __forceinline__ void shade_hit(const FrameParams& f, unsigned alb, in
 #pragma unroll
     for (int j = 0; j < 4; ++j) albf[j] = (float)((alb >> (8 * j)) & 255u) / 255.0f;
     if (f.shade == VT_SHADE_REFERENCE) {
-        const float a = shadowed ? 0.0f : (float)unorm8(0.3f) / 255.0f;
-        float sq[3], sc[3];
+        const float a = shadowed ? 0.0f : f.lit_a;
 #pragma unroll
-        for (int j = 0; j < 3; ++j) sq[j] = (float)unorm8(f.sun[j]) / 255.0f;
-        sky(f.sun, sq, sc);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) col[j] = albf[j] + a * sc[j];
+        for (int j = 0; j < 3; ++j) col[j] = albf[j] + a * f.lit_sky[j];
         col[3] = albf[3] + a * 1.0f;
         if (bounce_open) {
             float bc[3];
@@ -168,12 +170,11 @@ __device__ __forceinline__ void shade_hit(const FrameParams& f, unsigned alb, in
             for (int j = 0; j < 3; ++j) col[j] = col[j] + f.bounce_weight * (albf[j] * bc[j]);
         }
     } else if (f.shade == VT_SHADE_LAMBERT) {
-        float sn[3], nrm[3] = {0.0f, 0.0f, 0.0f};
+        float nrm[3] = {0.0f, 0.0f, 0.0f};
         nrm[0] = axis == 0 ? (pos_axis ? -1.0f : 1.0f) : 0.0f;
         nrm[1] = axis == 1 ? (pos_axis ? -1.0f : 1.0f) : 0.0f;
         nrm[2] = axis == 2 ? (pos_axis ? -1.0f : 1.0f) : 0.0f;
-        normalize3(f.sun, sn);
-        float ndl = dot3(nrm, sn);
+        float ndl = dot3(nrm, f.sun_n);
         if (ndl < 0.0f) ndl = 0.0f;
         const float vis = shadowed ? 0.0f : 1.0f;
         const float k = f.ambient + f.diffuse * ndl * vis;
@@ -212,6 +213,15 @@ __device__ __forceinline__ unsigned composite(const FrameParams& f, int px, int 
         }
     }
     return unorm8(col[0]) | (unorm8(col[1]) << 8) | (unorm8(col[2]) << 16) | (unorm8(col[3]) << 24);
+}
+
+// The per-frame constants of FrameParams (host side).
+inline void frame_constants(FrameParams& f) {
+    normalize3(f.sun, f.sun_n);
+    float sq[3];
+    for (int j = 0; j < 3; ++j) sq[j] = (float)unorm8(f.sun[j]) / 255.0f;
+    sky(f.sun, sq, f.lit_sky);
+    f.lit_a = (float)unorm8(0.3f) / 255.0f;
 }
 
 }  // namespace vt

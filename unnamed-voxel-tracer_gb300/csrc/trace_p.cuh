@@ -133,6 +133,13 @@ struct TraceHit {
 
 // Traverses one ray.  Returns true on a hit (filled into h; the material byte
 // is read only when MAT).
+//
+// Loop state: the cell c, the time tm[i] of the next plane on each axis (the
+// classic Amanatides-Woo tMax, always ptime of that plane), and which level of
+// the hierarchy is valid for the current cell: the chunk's coarse bit and the
+// brick's occupancy word are looked up again only after a crossing leaves the
+// chunk or the brick.  Inside an occupied brick a unit step is one argmin and
+// one axis update; an empty brick or chunk is left in one jump.
 template <bool STATS, bool CHECKED, bool MAT, class Coarse>
 __device__ __forceinline__ bool trace_p(const WorldView& w, const Coarse& coarse, const PRay& r, int max_steps,
                                         TraceHit& h, TraceCounters& cnt, unsigned* status) {
@@ -141,42 +148,49 @@ __device__ __forceinline__ bool trace_p(const WorldView& w, const Coarse& coarse
     int axis;
     if (!pray_start(r, w.dims, c, t, axis)) return false;
     if (max_steps <= 0) return false;
+    float tm[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) tm[i] = ptime(r, i, r.pos[i] ? c[i] + 1 : c[i]);
     int n = 0;
-    unsigned cached_wi = 0xFFFFFFFFu;
     unsigned long long word = 0ull;
+    unsigned ci = 0, wi = 0;
     unsigned last_cw = 0xFFFFFFFFu;
+    // 0: chunk of c not looked up; 1: chunk occupied, brick word not loaded;
+    // 2: brick word of c in `word`; 3: chunk of c is empty
+    int state = 0;
     for (;;) {
         if (STATS) cnt.iters++;
-        const unsigned ci = (unsigned)(c[0] >> 5) + (unsigned)w.cdim[0] * ((unsigned)(c[1] >> 5) + (unsigned)w.cdim[1] * (unsigned)(c[2] >> 5));
-        const unsigned cw = ci >> 6;
-        if (CHECKED && cw >= w.ncoarse) {
-            atomicOr(status, kStatusOob);
-            return false;
-        }
-        if (STATS && cw != last_cw) {
-            last_cw = cw;
-            cnt.coarse++;
-        }
-        int sh;
-        if (!((coarse(cw) >> (ci & 63u)) & 1ull)) {
-            sh = 5;
-        } else {
-            const unsigned bi = (unsigned)((c[0] >> 2) & 7) | ((unsigned)((c[1] >> 2) & 7) << 3) | ((unsigned)((c[2] >> 2) & 7) << 6);
-            const unsigned wi = ci * 512u + bi;
-            if (wi != cached_wi) {
-                if (CHECKED && wi >= w.nwords) {
-                    atomicOr(status, kStatusOob);
-                    return false;
-                }
-                word = __ldg(w.mask + wi);
-                cached_wi = wi;
-                if (STATS) cnt.mask++;
+        if (state == 0) {
+            ci = (unsigned)(c[0] >> 5) + (unsigned)w.cdim[0] * ((unsigned)(c[1] >> 5) + (unsigned)w.cdim[1] * (unsigned)(c[2] >> 5));
+            const unsigned cw = ci >> 6;
+            if (CHECKED && cw >= w.ncoarse) {
+                atomicOr(status, kStatusOob);
+                return false;
             }
-            if (word == 0ull) {
-                sh = 2;
-            } else {
+            if (STATS && cw != last_cw) {
+                last_cw = cw;
+                cnt.coarse++;
+            }
+            state = ((coarse(cw) >> (ci & 63u)) & 1ull) ? 1 : 3;
+        }
+        if (state == 1) {
+            wi = ci * 512u + ((unsigned)((c[0] >> 2) & 7) | ((unsigned)((c[1] >> 2) & 7) << 3) |
+                              ((unsigned)((c[2] >> 2) & 7) << 6));
+            if (CHECKED && wi >= w.nwords) {
+                atomicOr(status, kStatusOob);
+                return false;
+            }
+            word = __ldg(w.mask + wi);
+            if (STATS) cnt.mask++;
+            state = 2;
+        }
+        int sh = 5;
+        if (state == 2) {
+            sh = 2;
+            if (word != 0ull) {
                 const unsigned vb = (unsigned)(c[0] & 3) | ((unsigned)(c[1] & 3) << 2) | ((unsigned)(c[2] & 3) << 4);
-                if ((word >> vb) & 1ull) {
+                const unsigned half = (vb & 32u) ? (unsigned)(word >> 32) : (unsigned)word;
+                if ((half >> (vb & 31u)) & 1u) {
                     h.mat = MAT ? (unsigned)__ldg(w.mats + (size_t)wi * 64u + vb) : 0u;
                     h.t = t;
                     h.axis = axis;
@@ -189,38 +203,190 @@ __device__ __forceinline__ bool trace_p(const WorldView& w, const Coarse& coarse
                 sh = 0;
             }
         }
-        // Exit of the aligned 2^sh region that contains c.
+        if (sh == 0) {
+            // one unit crossing inside an occupied brick
+            const int e = tm[0] < tm[1] ? (tm[0] < tm[2] ? 0 : 2) : (tm[1] < tm[2] ? 1 : 2);
+            bool out = false, brick = false, chunk = false;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                if (i == e) {
+                    t = tm[i];
+                    c[i] += r.pos[i] ? 1 : -1;
+                    tm[i] = ptime(r, i, r.pos[i] ? c[i] + 1 : c[i]);
+                    const int lo = c[i] & 31;
+                    brick = (lo & 3) == (r.pos[i] ? 0 : 3);
+                    chunk = lo == (r.pos[i] ? 0 : 31);
+                    out = (unsigned)c[i] >= (unsigned)w.dims[i];
+                }
+            }
+            axis = e;
+            ++n;
+            if (n >= max_steps || out) break;
+            state = chunk ? 0 : (brick ? 1 : 2);
+        } else {
+            // leave the empty aligned 2^sh region that contains c in one jump
+            int K[3];
+            float tK[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const int base = c[i] & ~((1 << sh) - 1);
+                K[i] = r.pos[i] ? base + (1 << sh) : base;
+                tK[i] = ptime(r, i, K[i]);
+            }
+            const int e = tK[0] < tK[1] ? (tK[0] < tK[2] ? 0 : 2) : (tK[1] < tK[2] ? 1 : 2);
+            const float T = e == 0 ? tK[0] : (e == 1 ? tK[1] : tK[2]);
+            int crossings = 0;
+            bool chunk = sh == 5;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                if (i == e) {
+                    const int cn = r.pos[i] ? K[i] : K[i] - 1;
+                    crossings += abs(cn - c[i]);
+                    chunk = chunk || ((cn >> 5) != (c[i] >> 5));
+                    c[i] = cn;
+                    tm[i] = ptime(r, i, r.pos[i] ? cn + 1 : cn);
+                } else if (key_lt(tm[i], i, T, e)) {
+                    const int cn = advance_axis(r, i, c[i], K[i], T, e);
+                    crossings += abs(cn - c[i]);
+                    c[i] = cn;
+                    tm[i] = ptime(r, i, r.pos[i] ? cn + 1 : cn);
+                }
+            }
+            n += crossings;
+            t = T;
+            axis = e;
+            if (n >= max_steps) break;
+            if ((unsigned)c[0] >= (unsigned)w.dims[0] || (unsigned)c[1] >= (unsigned)w.dims[1] ||
+                (unsigned)c[2] >= (unsigned)w.dims[2])
+                break;
+            state = chunk ? 0 : 1;
+        }
+    }
+    if (STATS) cnt.steps += (unsigned)min(n, max_steps);
+    return false;
+}
+
+// The production traversal.  Same crossings, results and entry times as
+// trace_p (the jump argument holds for any empty axis-aligned box that contains
+// the current cell), with larger jumps and a cheaper unit step:
+//   - an empty chunk is left through the box of chunks within Chebyshev radius
+//     cdist - 1 (all empty), an empty brick through the box of bricks within
+//     radius bdist - 1;
+//   - inside an occupied brick only the next-plane index nk and time tm of the
+//     crossing axis change; the crossed plane's index tells whether the step
+//     left the brick (k % 4 == 0), the chunk (k % 32 == 0) or the grid, and the
+//     voxel's bit index moves by +-1, 4 or 16.
+// cdist is the per-chunk distance array (in shared memory in the kernels).
+template <bool MAT>
+__device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned char* cdist, const PRay& r,
+                                           int max_steps, TraceHit& h) {
+    int c[3];
+    float t;
+    int axis;
+    if (!pray_start(r, w.dims, c, t, axis)) return false;
+    if (max_steps <= 0) return false;
+    int nk[3];
+    float tm[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        nk[i] = r.pos[i] ? c[i] + 1 : c[i];
+        tm[i] = ptime(r, i, nk[i]);
+    }
+    int n = 0;
+    unsigned long long word = 0ull;
+    unsigned wi = 0, vb = 0;
+    int state = 0;  // 0: chunk of c unknown; 1: brick of c unknown; 2: c is inside the occupied brick `word`
+    for (;;) {
+        bool jump = false;
+        int sh = 0, rad = 0;
+        if (state == 0) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) c[i] = r.pos[i] ? nk[i] - 1 : nk[i];
+            const unsigned ci = (unsigned)(c[0] >> 5) + (unsigned)w.cdim[0] * ((unsigned)(c[1] >> 5) + (unsigned)w.cdim[1] * (unsigned)(c[2] >> 5));
+            const int dc = cdist[ci];
+            if (dc) {
+                jump = true;
+                sh = 5;
+                rad = dc;
+            } else {
+                state = 1;
+            }
+        }
+        if (state == 1) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) c[i] = r.pos[i] ? nk[i] - 1 : nk[i];
+            const unsigned ci = (unsigned)(c[0] >> 5) + (unsigned)w.cdim[0] * ((unsigned)(c[1] >> 5) + (unsigned)w.cdim[1] * (unsigned)(c[2] >> 5));
+            wi = ci * 512u + ((unsigned)((c[0] >> 2) & 7) | ((unsigned)((c[1] >> 2) & 7) << 3) | ((unsigned)((c[2] >> 2) & 7) << 6));
+            word = __ldg(w.mask + wi);
+            if (word == 0ull) {
+                jump = true;
+                sh = 2;
+                rad = __ldg(w.bdist + wi);
+            } else {
+                vb = (unsigned)(c[0] & 3) | ((unsigned)(c[1] & 3) << 2) | ((unsigned)(c[2] & 3) << 4);
+                state = 2;
+            }
+        }
+        if (!jump) {
+            // c is in an occupied brick: test the voxel, else one unit crossing
+            const unsigned half = (vb & 32u) ? (unsigned)(word >> 32) : (unsigned)word;
+            if ((half >> (vb & 31u)) & 1u) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) h.c[i] = r.pos[i] ? nk[i] - 1 : nk[i];
+                h.mat = MAT ? (unsigned)__ldg(w.mats + (size_t)wi * 64u + vb) : 0u;
+                h.t = t;
+                h.axis = axis;
+                return true;
+            }
+            const int e = tm[0] < tm[1] ? (tm[0] < tm[2] ? 0 : 2) : (tm[1] < tm[2] ? 1 : 2);
+            float T = tm[0];
+            int k = nk[0], xp = r.pos[0] ? w.dims[0] : 0;
+            unsigned dv = r.pos[0] ? 1u : 0xFFFFFFFFu;
+#pragma unroll
+            for (int i = 1; i < 3; ++i) {
+                if (i == e) {
+                    T = tm[i];
+                    k = nk[i];
+                    xp = r.pos[i] ? w.dims[i] : 0;
+                    dv = r.pos[i] ? (1u << (2 * i)) : (0u - (1u << (2 * i)));
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                if (i == e) {
+                    nk[i] += r.pos[i] ? 1 : -1;
+                    tm[i] = ptime(r, i, nk[i]);
+                }
+            }
+            t = T;
+            axis = e;
+            ++n;
+            if (n >= max_steps || k == xp) break;
+            if ((k & 3) == 0) state = (k & 31) == 0 ? 0 : 1;
+            else vb += dv;
+            continue;
+        }
+        // leave the empty box of radius rad - 1 units of 2^sh around the unit of c
         int K[3];
         float tK[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            const int base = (c[i] >> sh) << sh;
-            K[i] = r.pos[i] ? base + (1 << sh) : base;
+            const int u = c[i] >> sh;
+            K[i] = r.pos[i] ? (u + rad) * (1 << sh) : (u - (rad - 1)) * (1 << sh);
             tK[i] = ptime(r, i, K[i]);
         }
         const int e = tK[0] < tK[1] ? (tK[0] < tK[2] ? 0 : 2) : (tK[1] < tK[2] ? 1 : 2);
         const float T = e == 0 ? tK[0] : (e == 1 ? tK[1] : tK[2]);
         int crossings = 0;
-        if (sh) {
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                if (i != e) {
-                    const int nk = r.pos[i] ? c[i] + 1 : c[i];
-                    if (crossed(r, i, nk, T, e)) {
-                        const int cn = advance_axis(r, i, c[i], K[i], T, e);
-                        crossings += abs(cn - c[i]);
-                        c[i] = cn;
-                    }
-                }
-            }
-        }
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            if (i == e) {
-                const int cn = r.pos[i] ? K[i] : K[i] - 1;
-                crossings += abs(cn - c[i]);
-                c[i] = cn;
-            }
+            int cn = c[i];
+            if (i == e) cn = r.pos[i] ? K[i] : K[i] - 1;
+            else if (key_lt(tm[i], i, T, e)) cn = advance_axis(r, i, c[i], K[i], T, e);
+            crossings += abs(cn - c[i]);
+            c[i] = cn;
+            nk[i] = r.pos[i] ? cn + 1 : cn;
+            tm[i] = ptime(r, i, nk[i]);
         }
         n += crossings;
         t = T;
@@ -229,8 +395,8 @@ __device__ __forceinline__ bool trace_p(const WorldView& w, const Coarse& coarse
         if ((unsigned)c[0] >= (unsigned)w.dims[0] || (unsigned)c[1] >= (unsigned)w.dims[1] ||
             (unsigned)c[2] >= (unsigned)w.dims[2])
             break;
+        state = 0;
     }
-    if (STATS) cnt.steps += (unsigned)min(n, max_steps);
     return false;
 }
 

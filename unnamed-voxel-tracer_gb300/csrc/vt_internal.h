@@ -28,11 +28,19 @@ struct WorldView {
     const unsigned char* mats;          // 64 material bytes per brick, same order
     const unsigned long long* coarse;   // one bit per chunk
     const unsigned* palette;            // 256 RGBA8
+    const unsigned char* bdist;         // per brick: 0 if occupied, else Chebyshev distance in bricks
+                                        // to the nearest occupied brick, capped at kDistCap + 1
+    const unsigned char* cdist;         // per chunk: same, in chunks
     int dims[3];
     int cdim[3];                        // chunk counts
     unsigned nwords;                    // number of brick words
     unsigned ncoarse;                   // number of coarse words
+    unsigned nchunks;
 };
+
+// Cap of the empty-space distances: a stored value d >= 1 promises that every
+// brick (chunk) within Chebyshev radius d - 1 is empty.
+constexpr int kDistCap = 15;
 
 }  // namespace vt
 
@@ -58,6 +66,10 @@ struct vt_world {
     unsigned long long* d_coarse = nullptr;
     size_t ncoarse = 0;
     unsigned* d_palette = nullptr;
+    unsigned char* d_bdist = nullptr;
+    unsigned char* d_cdist = nullptr;
+    unsigned char* d_dtmp = nullptr;   // two brick-sized buffers for the distance passes
+    bool dist_dirty = true;            // distances rebuilt before the next render
     unsigned char* d_stage = nullptr;  // upload staging (grown on demand)
     size_t stage_bytes = 0;
 
@@ -67,6 +79,9 @@ struct vt_world {
         v.mats = d_mats;
         v.coarse = d_coarse;
         v.palette = d_palette;
+        v.bdist = d_bdist;
+        v.cdist = d_cdist;
+        v.nchunks = (unsigned)nchunks;
         for (int i = 0; i < 3; ++i) {
             v.dims[i] = dims[i];
             v.cdim[i] = cdim[i];
@@ -84,6 +99,8 @@ vt_status fail(vt_ctx* ctx, vt_status s, const std::string& msg, cudaError_t err
 vt_status check_cuda(vt_ctx* ctx, cudaError_t err, const char* what);
 // Context-owned device buffer of at least `bytes` (grown on demand).
 vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out);
+// Rebuilds the empty-space distances of a world on `st`.
+vt_status rebuild_distances(vt_world* w, cudaStream_t st);
 }  // namespace vt
 
 #define VT_CUDA(ctx, call)                                                      \

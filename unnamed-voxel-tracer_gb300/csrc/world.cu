@@ -85,6 +85,74 @@ __global__ void __launch_bounds__(512) k_set_voxel(WorldView w, unsigned long lo
     }
 }
 
+// Empty-space distances.  The Chebyshev distance from a brick (chunk) to the
+// nearest occupied one is separable: min over b' of max(|dx|, |dy|, |dz|)
+// = min_dz max(|dz|, min_dy max(|dy|, min_dx max(|dx|, occ(b')))).  Each pass
+// is one of those 1-D min-max filters over a window of +-kDistCap; values are
+// capped at kDistCap + 1 ("nothing occupied within kDistCap").  Cells outside
+// the grid count as empty.
+__device__ __forceinline__ unsigned brick_index(int bx, int by, int bz, int CX, int CY) {
+    const unsigned ci = (unsigned)(bx >> 3) + (unsigned)CX * ((unsigned)(by >> 3) + (unsigned)CY * (unsigned)(bz >> 3));
+    return ci * 512u + (unsigned)((bx & 7) | ((by & 7) << 3) | ((bz & 7) << 6));
+}
+
+// level 0: bricks (grid = 8 * chunk counts), level 1: chunks.  pass 0 reads
+// occupancy from the mask words / coarse bits, later passes read `in`.
+__global__ void k_dist_pass(const unsigned long long* __restrict__ mask, const unsigned long long* __restrict__ coarse,
+                            const unsigned char* __restrict__ in, unsigned char* __restrict__ out, int level, int axis,
+                            int CX, int CY, int CZ) {
+    const int gx = level == 0 ? CX * 8 : CX, gy = level == 0 ? CY * 8 : CY, gz = level == 0 ? CZ * 8 : CZ;
+    const size_t total = (size_t)gx * gy * gz;
+    for (size_t lin = blockIdx.x * (size_t)blockDim.x + threadIdx.x; lin < total; lin += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(lin % gx), y = (int)((lin / gx) % gy), z = (int)(lin / ((size_t)gx * gy));
+        const int g[3] = {gx, gy, gz};
+        int p[3] = {x, y, z};
+        const int u = p[axis];
+        int best = kDistCap + 1;
+        for (int dd = -kDistCap; dd <= kDistCap; ++dd) {
+            const int q = u + dd;
+            if (q < 0 || q >= g[axis]) continue;
+            p[axis] = q;
+            unsigned idx;
+            if (level == 0) idx = brick_index(p[0], p[1], p[2], CX, CY);
+            else idx = (unsigned)p[0] + (unsigned)CX * ((unsigned)p[1] + (unsigned)CY * (unsigned)p[2]);
+            int v;
+            if (axis == 0) {
+                const bool occ = level == 0 ? mask[idx] != 0ull : ((coarse[idx >> 6] >> (idx & 63u)) & 1ull) != 0ull;
+                v = occ ? 0 : kDistCap + 1;
+            } else {
+                v = in[idx];
+            }
+            const int m = max(abs(dd), v);
+            best = min(best, m);
+        }
+        p[axis] = u;
+        const unsigned oidx = level == 0 ? brick_index(x, y, z, CX, CY)
+                                         : (unsigned)x + (unsigned)CX * ((unsigned)y + (unsigned)CY * (unsigned)z);
+        out[oidx] = (unsigned char)best;
+    }
+}
+
+vt_status rebuild_distances(vt_world* w, cudaStream_t st) {
+    const int CX = w->cdim[0], CY = w->cdim[1], CZ = w->cdim[2];
+    const size_t nb = w->nchunks * kBricksPerChunk;
+    unsigned char* a = w->d_dtmp;
+    unsigned char* b = w->d_dtmp + nb;
+    const int threads = 256;
+    auto blocks = [&](size_t n) { return (unsigned)std::min<size_t>((n + threads - 1) / threads, 65535u * 4u); };
+    // bricks: x -> a, y -> b, z -> bdist
+    k_dist_pass<<<blocks(nb), threads, 0, st>>>(w->d_mask, w->d_coarse, nullptr, a, 0, 0, CX, CY, CZ);
+    k_dist_pass<<<blocks(nb), threads, 0, st>>>(w->d_mask, w->d_coarse, a, b, 0, 1, CX, CY, CZ);
+    k_dist_pass<<<blocks(nb), threads, 0, st>>>(w->d_mask, w->d_coarse, b, w->d_bdist, 0, 2, CX, CY, CZ);
+    // chunks
+    k_dist_pass<<<blocks(w->nchunks), threads, 0, st>>>(w->d_mask, w->d_coarse, nullptr, a, 1, 0, CX, CY, CZ);
+    k_dist_pass<<<blocks(w->nchunks), threads, 0, st>>>(w->d_mask, w->d_coarse, a, b, 1, 1, CX, CY, CZ);
+    k_dist_pass<<<blocks(w->nchunks), threads, 0, st>>>(w->d_mask, w->d_coarse, b, w->d_cdist, 1, 2, CX, CY, CZ);
+    VT_CUDA(w->ctx, cudaGetLastError());
+    w->dist_dirty = false;
+    return VT_OK;
+}
+
 static vt_status ensure_stage(vt_world* w, size_t bytes) {
     if (bytes <= w->stage_bytes) return VT_OK;
     if (w->d_stage) {
@@ -104,6 +172,9 @@ static void free_world(vt_world* w) {
     if (w->d_coarse) cudaFree(w->d_coarse);
     if (w->d_palette) cudaFree(w->d_palette);
     if (w->d_stage) cudaFree(w->d_stage);
+    if (w->d_bdist) cudaFree(w->d_bdist);
+    if (w->d_cdist) cudaFree(w->d_cdist);
+    if (w->d_dtmp) cudaFree(w->d_dtmp);
     delete w;
 }
 
@@ -137,6 +208,9 @@ vt_status vt_world_create(vt_ctx* ctx, const vt_world_desc* desc, vt_world** out
         (e = cudaMalloc(&w->d_mats, w->nchunks * (size_t)kChunkBytes)) != cudaSuccess ||
         (e = cudaMalloc(&w->d_coarse, w->ncoarse * 8)) != cudaSuccess ||
         (e = cudaMalloc(&w->d_palette, 256 * sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_bdist, w->nchunks * kBricksPerChunk)) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_cdist, (w->nchunks + 15) / 16 * 16)) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_dtmp, 2 * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
         (e = cudaMemset(w->d_mask, 0, w->nchunks * kBricksPerChunk * 8)) != cudaSuccess ||
         (e = cudaMemset(w->d_mats, 0, w->nchunks * (size_t)kChunkBytes)) != cudaSuccess ||
         (e = cudaMemset(w->d_coarse, 0, w->ncoarse * 8)) != cudaSuccess) {
@@ -166,6 +240,7 @@ vt_status vt_world_clear(vt_world* w, vt_stream stream) {
     VT_CUDA(w->ctx, cudaMemsetAsync(w->d_mask, 0, w->nchunks * kBricksPerChunk * 8, s));
     VT_CUDA(w->ctx, cudaMemsetAsync(w->d_mats, 0, w->nchunks * (size_t)kChunkBytes, s));
     VT_CUDA(w->ctx, cudaMemsetAsync(w->d_coarse, 0, w->ncoarse * 8, s));
+    w->dist_dirty = true;
     return VT_OK;
 }
 
@@ -182,6 +257,7 @@ vt_status vt_world_upload_dense(vt_world* w, const uint8_t* h_materials, size_t 
                                                         make_int3(0, 0, 0), make_int3(0, 0, 0),
                                                         make_int3(w->cdim[0], w->cdim[1], w->cdim[2]));
     VT_CUDA(w->ctx, cudaGetLastError());
+    w->dist_dirty = true;
     // the staging buffer is reused by the next upload on any stream
     VT_CUDA(w->ctx, cudaStreamSynchronize(st));
     return VT_OK;
@@ -200,6 +276,7 @@ vt_status vt_world_upload_chunk(vt_world* w, int32_t cx, int32_t cy, int32_t cz,
     k_build_chunks<<<1, 512, 0, st>>>(w->view(), w->d_mask, w->d_mats, w->d_coarse, w->d_stage, make_int3(32, 32, 32),
                                       make_int3(cx * 32, cy * 32, cz * 32), make_int3(cx, cy, cz), make_int3(1, 1, 1));
     VT_CUDA(w->ctx, cudaGetLastError());
+    w->dist_dirty = true;
     VT_CUDA(w->ctx, cudaStreamSynchronize(st));
     return VT_OK;
 }
@@ -210,6 +287,7 @@ vt_status vt_world_set_voxel(vt_world* w, int32_t x, int32_t y, int32_t z, uint8
         return fail(w->ctx, VT_ERR_ARG, "voxel coordinate out of range");
     k_set_voxel<<<1, 512, 0, (cudaStream_t)stream>>>(w->view(), w->d_mask, w->d_mats, w->d_coarse, x, y, z, material);
     VT_CUDA(w->ctx, cudaGetLastError());
+    w->dist_dirty = true;
     return VT_OK;
 }
 
