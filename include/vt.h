@@ -217,6 +217,28 @@ typedef struct {
 vt_status vt_render_stats(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
                           const vt_params* params, vt_stats* out, vt_stream stream);
 
+/* ------------------------------------------------------------------ tuning
+ * Launch configuration of the render kernels (no counterpart in the
+ * reference, whose dispatch shape is fixed at 32x32 groups, game.zig:241-248).
+ * Every configuration produces identical records; only speed differs. */
+#define VT_KERNEL_TILE  0 /* one thread per pixel, warp = pixel tile */
+#define VT_KERNEL_QUEUE 1 /* persistent warps refilling lanes from a pixel queue */
+typedef struct {
+    int32_t kernel;       /* VT_KERNEL_* */
+    int32_t warp_tile_w;  /* VT_KERNEL_TILE: a warp's tile is w x (32/w) pixels, w in {8, 16, 32} */
+    int32_t occupancy;    /* VT_KERNEL_TILE: 1 = register budget capped for 40 warps per SM */
+    int32_t batch;        /* VT_KERNEL_QUEUE: parked lanes (1..32) that trigger a refill pass */
+} vt_tuning;
+vt_status vt_set_tuning(vt_ctx* ctx, const vt_tuning* tuning);
+vt_status vt_get_tuning(vt_ctx* ctx, vt_tuning* tuning);
+/* Times every candidate configuration on this frame (reps launches each,
+ * CUDA events on the context's stream), keeps the fastest in the context and
+ * returns it with its mean time in ms.  With a non-NULL cache_path the choice
+ * is looked up first and recorded afterwards in that text file, keyed by GPU
+ * name, world size, image size and ray kinds. */
+vt_status vt_autotune(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* params,
+                      int32_t reps, const char* cache_path, vt_tuning* best, float* best_ms);
+
 /* traceMap over an explicit ray list (map.glsl:83-168 semantics on the mode-P
  * world, no clipping beyond the grid box): d_origins/d_dirs are n*3 floats. */
 vt_status vt_trace_rays(vt_ctx* ctx, const vt_world* world, const float* d_origins,

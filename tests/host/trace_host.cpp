@@ -109,8 +109,22 @@ extern "C" int ht_trace_rays(const int32_t dims[3], const uint8_t* dense, const 
         vt::pray_init(r, origins + 3 * i, dirs + 3 * i);
         vt::TraceHit h;
         vt::TraceCounters cnt;
-        bool hit = fast ? vt::trace_fast<true>(w, w.cdist, r, max_steps, h)
-                        : vt::trace_p<true, true, true>(w, vt::CoarseGlobal{w.coarse}, r, max_steps, h, cnt, &status);
+        bool hit;
+        if (fast) {
+            // the production walk, one step at a time; counters[0] = steps taken
+            vt::Walker wk;
+            hit = false;
+            if (wk.start(w, r.o, r.d, max_steps)) {
+                int s;
+                do {
+                    s = wk.step<true>(w, w.cdist, h);
+                    counters[0]++;
+                } while (s == vt::Walker::kMore);
+                hit = s == vt::Walker::kHit;
+            }
+        } else {
+            hit = vt::trace_p<true, true, true>(w, vt::CoarseGlobal{w.coarse}, r, max_steps, h, cnt, &status);
+        }
         uint32_t* o = out + 4 * i;
         if (hit) {
             const int e = h.axis;

@@ -94,17 +94,62 @@ def test_config0_frame(vt, oracle, ctx, shade):
     assert (gpu["flags"] & vt.HIT_PRIMARY).mean() > 0.3
 
 
-def test_config1_world_primary_shadow(vt, oracle, ctx):
+TUNINGS = [dict(kernel=0, warp_tile_w=tw, occupancy=o) for tw in (8, 16, 32) for o in (0, 1)] + \
+          [dict(kernel=1, batch=b) for b in (1, 16, 32)]
+
+
+@pytest.fixture
+def tuned(ctx):
+    yield ctx
+    ctx.set_tuning()  # back to the default configuration
+
+
+@pytest.mark.parametrize("tuning", TUNINGS, ids=lambda t: "-".join(f"{k}{v}" for k, v in t.items()))
+def test_config1_world_primary_shadow(vt, oracle, tuned, tuning):
     """512x256x512 with 200 trees; primary + shadow, reference shading
-    (reduced image so the oracle finishes in seconds)."""
+    (reduced image so the oracle finishes in seconds), under every launch
+    configuration the autotuner may pick."""
     d = vt.gen_desc((512, 256, 512), seed=1, trees=200)
     mats = vt.gen_world(d)
     sun = vt.gen_sun(1)
-    for cs in range(3):
-        cam = vt.gen_camera(d, cs, 320, 180)
+    tuned.set_tuning(**tuning)
+    for cs in range(2):
+        cam = vt.gen_camera(d, cs, 333, 187)   # partial tiles at the edges
         p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=sun)
-        gpu, ref, _ = render_both(vt, oracle, ctx, mats, cam, p)
+        gpu, ref, _ = render_both(vt, oracle, tuned, mats, cam, p)
         compare(gpu, ref)
+
+
+def test_repeated_frames_are_identical(vt, tuned):
+    """The pixel queue hands pixels out in a different order every launch;
+    the records must not depend on it, nor on the configuration."""
+    d = vt.gen_desc((256, 128, 256), seed=3, trees=40)
+    w = make_world(vt, tuned, vt.gen_world(d))
+    cam = vt.gen_camera(d, 1, 640, 360)
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW | vt.RAYS_BOUNCE, sun_dir=vt.gen_sun(3))
+    first = vt.render_host(tuned, w, cam, p)
+    tuned.set_tuning(kernel=vt.KERNEL_QUEUE, batch=16)
+    for _ in range(4):
+        assert np.array_equal(vt.render_host(tuned, w, cam, p), first)
+    w.close()
+
+
+def test_autotune_picks_a_candidate_and_caches_it(vt, tuned, tmp_path):
+    d = vt.gen_desc((256, 128, 256), seed=5, trees=20)
+    w = make_world(vt, tuned, vt.gen_world(d))
+    cam = vt.gen_camera(d, 0, 480, 270)
+    p = vt.default_params()
+    cache = str(tmp_path / "tune.txt")
+    best, ms = tuned.autotune(w, cam, p, reps=2, cache_path=cache)
+    assert ms > 0 and tuned.get_tuning() == best
+    tuned.set_tuning()
+    again, ms2 = tuned.autotune(w, cam, p, reps=2, cache_path=cache)   # served from the cache
+    assert again == best and ms2 == pytest.approx(ms)
+    assert len(open(cache).read().splitlines()) == 1
+    ref = vt.render_host(tuned, w, cam, p)
+    tuned.set_tuning()
+    assert np.array_equal(vt.render_host(tuned, w, cam, p), ref)
+    w.close()
 
 
 def test_bounce_rays(vt, oracle, ctx):

@@ -84,6 +84,7 @@ vt_status vt_ctx_create(int32_t device, vt_ctx** out) {
         if ((e = cudaMalloc(&ctx->d_status, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
         if ((e = cudaMemset(ctx->d_status, 0, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMemset"); break; }
         if ((e = cudaMalloc(&ctx->d_counters, kNumCounters * sizeof(unsigned long long))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
+        if ((e = cudaMalloc(&ctx->d_work, kWorkSlots * sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
         // blocking stream: *_host calls order after work queued on the legacy default stream
         if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamDefault)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaStreamCreate"); break; }
     } while (0);
@@ -102,6 +103,7 @@ vt_status vt_ctx_destroy(vt_ctx* ctx) {
     if (ctx->d_scratch) cudaFree(ctx->d_scratch);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->d_work) cudaFree(ctx->d_work);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return VT_OK;

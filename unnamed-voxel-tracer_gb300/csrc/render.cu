@@ -15,10 +15,8 @@
 
 namespace vt {
 
-// Pixel tile of a 256-thread block: 16 x 16 pixels, each warp an 8 x 4 tile
-// so that a warp's rays start close together and share brick words in L1.
-constexpr int kTileW = 16;
-constexpr int kTileH = 16;
+// 256-thread blocks; each warp traces a compact pixel tile so that its rays
+// start close together and share brick words in L1.
 constexpr int kBlock = 256;
 constexpr size_t kMaxSharedCoarse = 48 * 1024;
 
@@ -128,9 +126,19 @@ __device__ __forceinline__ void flush_counters(PixelCounters& pc, unsigned long 
     }
 }
 
-template <bool STATS, bool CHECKED, bool SMEM>
-__global__ void __launch_bounds__(kBlock) k_render(WorldView w, FrameParams f, uint4* __restrict__ out,
-                                                   unsigned* status, unsigned long long* counters) {
+// One thread per pixel.  A warp covers a TW x (32 / TW) pixel tile; the
+// 256-thread block covers max(16, TW) pixels across.  OCC caps the register
+// budget so that 5 blocks (40 warps) fit on an SM.
+template <int TW>
+struct BlockTile {
+    static constexpr int kW = TW < 16 ? 16 : TW;     // block tile width
+    static constexpr int kWarpsX = kW / TW;
+    static constexpr int kH = (8 / kWarpsX) * (32 / TW);
+};
+
+template <bool STATS, bool CHECKED, bool SMEM, int TW, bool OCC>
+__global__ void __launch_bounds__(kBlock, OCC ? 5 : 1) k_render(WorldView w, FrameParams f, uint4* __restrict__ out,
+                                                               unsigned* status, unsigned long long* counters) {
     // shared copy of the coarse level: per-chunk distances (production) or
     // coarse bits (model traversal)
     extern __shared__ uint4 s_dyn[];
@@ -146,8 +154,9 @@ __global__ void __launch_bounds__(kBlock) k_render(WorldView w, FrameParams f, u
         __syncthreads();
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int px = blockIdx.x * kTileW + (warp & 1) * 8 + (lane & 7);
-    const int py = blockIdx.y * kTileH + (warp >> 1) * 4 + (lane >> 3);
+    using BT = BlockTile<TW>;
+    const int px = blockIdx.x * BT::kW + (warp % BT::kWarpsX) * TW + (lane % TW);
+    const int py = blockIdx.y * BT::kH + (warp / BT::kWarpsX) * (32 / TW) + (lane / TW);
     PixelCounters pc;
 #pragma unroll
     for (int k = 0; k < kNumCounters; ++k) pc.v[k] = 0;
@@ -189,6 +198,163 @@ __global__ void __launch_bounds__(kBlock) k_trace_rays(WorldView w, const float*
     }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent render kernel (production path).
+//
+// A one-ray-per-thread launch leaves lanes idle: a warp runs until its longest
+// primary ray ends, then again until its longest shadow ray ends, while lanes
+// whose ray ended (or whose primary missed) wait.  Here every lane owns one
+// pixel at a time and walks its primary, shadow and bounce rays in one loop;
+// a lane whose pixel is finished takes the next pixel from the warp's batch of
+// 32 queue entries, and the warp grabs a new batch from a global counter when
+// the batch is used up.  Queue entries walk the image in 8 x 4 pixel tiles, so
+// the lanes of a warp still trace neighbouring pixels.
+constexpr int kPersistBlock = 128;
+constexpr unsigned kGrab = 32;
+
+__device__ __forceinline__ void pixel_of(unsigned idx, unsigned tiles_x, int& px, int& py) {
+    const unsigned tile = idx >> 5, l = idx & 31u;
+    px = (int)((tile % tiles_x) * 8u + (l & 7u));
+    py = (int)((tile / tiles_x) * 4u + (l >> 3));
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(kPersistBlock) k_render_persist(WorldView w, FrameParams f, uint4* __restrict__ out,
+                                                                  unsigned* __restrict__ work, unsigned total,
+                                                                  unsigned tiles_x, int batch) {
+    extern __shared__ uint4 s_dyn[];
+    const unsigned char* cd = w.cdist;
+    if (SMEM) {
+        const uint4* src = reinterpret_cast<const uint4*>(w.cdist);
+        for (unsigned i = threadIdx.x; i < (w.nchunks + 15u) / 16u; i += blockDim.x) s_dyn[i] = __ldg(src + i);
+        __syncthreads();
+        cd = reinterpret_cast<const unsigned char*>(s_dyn);
+    }
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned below = (1u << lane) - 1u;
+    unsigned bnext = 0, bend = 0;  // the warp's batch of queue entries (warp-uniform)
+    // per lane: the ray being walked (kind 1 primary, 2 shadow, 3 bounce), or
+    // parked with the result of the ray that ended (res), or without a pixel
+    int kind = 0, res = 0;
+    bool active = false, retired = false;
+    int px = 0, py = 0;
+    Walker wk;
+    unsigned voxel = 0, face = 0, mat = 0, flags = 0;
+    float thit = 0.0f, so[3] = {0.0f, 0.0f, 0.0f}, nrm[3] = {0.0f, 0.0f, 0.0f}, bdir[3] = {0.0f, 0.0f, 0.0f};
+    int e_hit = 0;
+    bool pe_hit = false;
+
+    for (;;) {
+        if (active) {
+            TraceHit h;
+            const int s = wk.step<true>(w, cd, h);
+            if (s != Walker::kMore) {
+                active = false;
+                res = s;
+                if (kind == 1 && s == Walker::kHit) {
+                    voxel = (unsigned)h.c[0] + (unsigned)w.dims[0] * ((unsigned)h.c[1] + (unsigned)w.dims[1] * (unsigned)h.c[2]);
+                    thit = h.t;
+                    e_hit = h.axis;
+                    mat = h.mat;
+                }
+            }
+        }
+        const unsigned parked = __ballot_sync(0xFFFFFFFFu, !active);
+        if (__popc(parked) < batch) continue;
+        if (parked == 0xFFFFFFFFu && __all_sync(0xFFFFFFFFu, retired)) break;
+
+        // ---- one transition pass for every parked lane ----
+        bool need_pixel = false;
+        if (!active && !retired) {
+            bool finish = false;
+            if (kind == 0) {
+                need_pixel = true;
+            } else if (kind == 1) {
+                if (res == Walker::kMiss) {
+                    float o[3], d[3], col[4];
+                    primary_ray(f, px, py, o, d);
+                    shade_miss(f, d, col);
+                    const unsigned rgba = f.shade == VT_SHADE_NONE ? 0u : composite(f, px, py, col);
+                    out[(size_t)py * f.width + px] = make_uint4(0xFFFFFFFFu, __float_as_uint(-1.0f), rgba, 0xFFu);
+                    need_pixel = true;
+                } else {
+                    flags = VT_HIT_PRIMARY;
+                    pe_hit = e_hit == 0 ? wk.r.pos[0] : (e_hit == 1 ? wk.r.pos[1] : wk.r.pos[2]);
+                    face = 2u * (unsigned)e_hit + (pe_hit ? 0u : 1u);
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        nrm[j] = (j == e_hit) ? (pe_hit ? -1.0f : 1.0f) : 0.0f;
+                        so[j] = __fmaf_rn(wk.r.d[j], thit, wk.r.o[j]);
+                        if (j == e_hit) so[j] = so[j] + nrm[j] * 0.001f;
+                    }
+                    kind = 2;
+                    if (f.rays & VT_RAYS_SHADOW) active = wk.start(w, so, f.sun, f.shadow_max_steps);
+                    res = Walker::kMiss;  // a shadow ray that cannot start is unblocked
+                }
+            }
+            if (!active && kind == 2) {
+                if (res == Walker::kHit) flags |= VT_HIT_SHADOWED;
+                kind = 3;
+                if (f.rays & VT_RAYS_BOUNCE) {
+                    unsigned seed = ((unsigned)px * 1973u + (unsigned)py * 9277u) ^ f.seed;
+                    cosine_hemisphere(nrm, seed, bdir);
+                    active = wk.start(w, so, bdir, f.bounce_max_steps);
+                    res = Walker::kMiss;
+                } else {
+                    finish = true;
+                }
+            } else if (!active && kind == 3) {
+                if (res == Walker::kHit) flags |= VT_HIT_BOUNCE;
+                finish = true;
+            }
+            if (finish) {
+                const unsigned alb = __ldg(w.palette + mat);
+                float col[4];
+                shade_hit(f, alb, e_hit, pe_hit, (flags & VT_HIT_SHADOWED) != 0,
+                          (f.rays & VT_RAYS_BOUNCE) && !(flags & VT_HIT_BOUNCE), bdir, col);
+                const unsigned rgba = f.shade == VT_SHADE_NONE ? alb : composite(f, px, py, col);
+                out[(size_t)py * f.width + px] =
+                    make_uint4(voxel, __float_as_uint(thit), rgba, face | (mat << 8) | (flags << 16));
+                need_pixel = true;
+            }
+        }
+        // ---- refill lanes without a pixel from the queue ----
+        unsigned need = __ballot_sync(0xFFFFFFFFu, need_pixel);
+        while (need) {
+            if (bnext == bend) {
+                unsigned b = 0;
+                if (lane == 0) b = atomicAdd(work, kGrab);
+                b = __shfl_sync(0xFFFFFFFFu, b, 0);
+                bnext = b;
+                bend = b + kGrab;
+            }
+            const unsigned avail = bend - bnext;
+            const unsigned rank = __popc(need & below);
+            if (need_pixel && rank < avail) {
+                const unsigned idx = bnext + rank;
+                need_pixel = false;
+                kind = 0;
+                if (idx >= total) {
+                    retired = true;
+                } else {
+                    pixel_of(idx, tiles_x, px, py);
+                    if (px < f.width && py < f.height) {
+                        float o[3], d[3];
+                        primary_ray(f, px, py, o, d);
+                        kind = 1;
+                        active = wk.start(w, o, d, f.max_steps);
+                        res = Walker::kMiss;  // a primary that cannot start misses
+                    }
+                }
+            }
+            bnext += min(avail, (unsigned)__popc(need));
+            // lanes whose entry was outside the image or whose primary missed
+            // the grid at once take another entry in the next transition
+            need = __ballot_sync(0xFFFFFFFFu, need_pixel);
+        }
+    }
+}
+
 FrameParams make_frame(const vt_camera* cam, const vt_params* p) {
     FrameParams f;
     for (int j = 0; j < 3; ++j) {
@@ -227,7 +393,6 @@ static vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_came
                                uint4* d_out, cudaStream_t stream, bool stats) {
     const FrameParams f = make_frame(cam, p);
     const WorldView w = world->view();
-    const dim3 grid((cam->width + kTileW - 1) / kTileW, (cam->height + kTileH - 1) / kTileH);
     const bool checked = (p->flags & VT_FLAG_CHECKED) != 0;
     const size_t smem = (stats || checked) ? (size_t)w.ncoarse * sizeof(unsigned long long)
                                            : (size_t)((w.nchunks + 15u) / 16u) * 16u;
@@ -237,17 +402,51 @@ static vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_came
         if (s) return s;
     }
     const size_t sm = use_smem ? smem : 0;
-#define VT_LAUNCH(S, C, M) k_render<S, C, M><<<grid, kBlock, sm, stream>>>(w, f, d_out, ctx->d_status, ctx->d_counters)
-    if (stats) {
-        if (use_smem) VT_LAUNCH(true, true, true);
-        else VT_LAUNCH(true, true, false);
-    } else if (checked) {
-        if (use_smem) VT_LAUNCH(false, true, true);
-        else VT_LAUNCH(false, true, false);
-    } else {
-        if (use_smem) VT_LAUNCH(false, false, true);
-        else VT_LAUNCH(false, false, false);
+    const vt_tuning& tu = ctx->tuning;
+    if (!stats && !checked && tu.kernel == VT_KERNEL_QUEUE) {
+        // persistent kernel over a pixel queue; the queue counter is one slot
+        // of the context's ring, zeroed on this stream before the launch
+        if (ctx->persist_blocks == 0) {
+            int nb = 0;
+            VT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_render_persist<true>, kPersistBlock,
+                                                                      kMaxSharedCoarse));
+            ctx->persist_blocks = nb > 0 ? nb : 1;
+        }
+        unsigned* counter = ctx->d_work + (ctx->work_slot++ % kWorkSlots);
+        VT_CUDA(ctx, cudaMemsetAsync(counter, 0, sizeof(unsigned), stream));
+        const unsigned tiles_x = (unsigned)(cam->width + 7) / 8u, tiles_y = (unsigned)(cam->height + 3) / 4u;
+        const unsigned total = tiles_x * tiles_y * 32u;
+        const unsigned blocks = (unsigned)(ctx->sm_count * ctx->persist_blocks);
+        const int batch = tu.batch;
+        if (use_smem)
+            k_render_persist<true><<<blocks, kPersistBlock, sm, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
+        else
+            k_render_persist<false><<<blocks, kPersistBlock, 0, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
+        VT_CUDA(ctx, cudaGetLastError());
+        return VT_OK;
     }
+#define VT_LAUNCH(S, C, M, TW, O)                                                                               \
+    k_render<S, C, M, TW, O><<<dim3((cam->width + BlockTile<TW>::kW - 1) / BlockTile<TW>::kW,                   \
+                                    (cam->height + BlockTile<TW>::kH - 1) / BlockTile<TW>::kH),                 \
+                               kBlock, sm, stream>>>(w, f, d_out, ctx->d_status, ctx->d_counters)
+#define VT_LAUNCH_M(S, C, TW, O)      \
+    if (use_smem) VT_LAUNCH(S, C, true, TW, O); \
+    else VT_LAUNCH(S, C, false, TW, O)
+    if (stats) {
+        VT_LAUNCH_M(true, true, 8, false);
+    } else if (checked) {
+        VT_LAUNCH_M(false, true, 8, false);
+    } else if (tu.warp_tile_w == 16) {
+        if (tu.occupancy) { VT_LAUNCH_M(false, false, 16, true); }
+        else { VT_LAUNCH_M(false, false, 16, false); }
+    } else if (tu.warp_tile_w == 32) {
+        if (tu.occupancy) { VT_LAUNCH_M(false, false, 32, true); }
+        else { VT_LAUNCH_M(false, false, 32, false); }
+    } else {
+        if (tu.occupancy) { VT_LAUNCH_M(false, false, 8, true); }
+        else { VT_LAUNCH_M(false, false, 8, false); }
+    }
+#undef VT_LAUNCH_M
 #undef VT_LAUNCH
     VT_CUDA(ctx, cudaGetLastError());
     return VT_OK;

@@ -276,27 +276,45 @@ __device__ __forceinline__ bool trace_p(const WorldView& w, const Coarse& coarse
 //     crossing axis change; the crossed plane's index tells whether the step
 //     left the brick (k % 4 == 0), the chunk (k % 32 == 0) or the grid, and the
 //     voxel's bit index moves by +-1, 4 or 16.
+// The walk is resumable one iteration at a time (step), so that a persistent
+// kernel can interleave rays of different pixels and kinds in one warp.
 // cdist is the per-chunk distance array (in shared memory in the kernels).
-template <bool MAT>
-__device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned char* cdist, const PRay& r,
-                                           int max_steps, TraceHit& h) {
-    int c[3];
-    float t;
-    int axis;
-    if (!pray_start(r, w.dims, c, t, axis)) return false;
-    if (max_steps <= 0) return false;
-    int nk[3];
-    float tm[3];
+struct Walker {
+    PRay r;
+    int max_steps;
+    int c[3];       // current cell (valid in states 0 and 1)
+    int nk[3];      // next plane index per axis
+    float tm[3];    // its crossing time
+    int n;          // unit crossings made
+    float t;        // entry time of the current cell
+    int axis;       // axis of the crossing that entered it
+    unsigned long long word;
+    unsigned wi, vb;
+    int state;      // 0: chunk of c unknown; 1: brick of c unknown; 2: in the occupied brick `word`
+
+    enum { kMore = 0, kHit = 1, kMiss = 2 };
+
+    // Sets up the walk; false if the ray misses the grid or may take no step.
+    __device__ __forceinline__ bool start(const WorldView& w, const float o[3], const float d[3], int steps) {
+        pray_init(r, o, d);
+        max_steps = steps;
+        if (!pray_start(r, w.dims, c, t, axis)) return false;
+        if (steps <= 0) return false;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        nk[i] = r.pos[i] ? c[i] + 1 : c[i];
-        tm[i] = ptime(r, i, nk[i]);
+        for (int i = 0; i < 3; ++i) {
+            nk[i] = r.pos[i] ? c[i] + 1 : c[i];
+            tm[i] = ptime(r, i, nk[i]);
+        }
+        n = 0;
+        word = 0ull;
+        wi = vb = 0;
+        state = 0;
+        return true;
     }
-    int n = 0;
-    unsigned long long word = 0ull;
-    unsigned wi = 0, vb = 0;
-    int state = 0;  // 0: chunk of c unknown; 1: brick of c unknown; 2: c is inside the occupied brick `word`
-    for (;;) {
+
+    // One iteration: a lookup plus a jump, or a voxel test plus a unit step.
+    template <bool MAT>
+    __device__ __forceinline__ int step(const WorldView& w, const unsigned char* cdist, TraceHit& h) {
         bool jump = false;
         int sh = 0, rad = 0;
         if (state == 0) {
@@ -328,7 +346,7 @@ __device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned ch
             }
         }
         if (!jump) {
-            // c is in an occupied brick: test the voxel, else one unit crossing
+            // inside an occupied brick: test the voxel, else one unit crossing
             const unsigned half = (vb & 32u) ? (unsigned)(word >> 32) : (unsigned)word;
             if ((half >> (vb & 31u)) & 1u) {
 #pragma unroll
@@ -336,7 +354,7 @@ __device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned ch
                 h.mat = MAT ? (unsigned)__ldg(w.mats + (size_t)wi * 64u + vb) : 0u;
                 h.t = t;
                 h.axis = axis;
-                return true;
+                return kHit;
             }
             const int e = tm[0] < tm[1] ? (tm[0] < tm[2] ? 0 : 2) : (tm[1] < tm[2] ? 1 : 2);
             float T = tm[0];
@@ -361,10 +379,10 @@ __device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned ch
             t = T;
             axis = e;
             ++n;
-            if (n >= max_steps || k == xp) break;
+            if (n >= max_steps || k == xp) return kMiss;
             if ((k & 3) == 0) state = (k & 31) == 0 ? 0 : 1;
             else vb += dv;
-            continue;
+            return kMore;
         }
         // leave the empty box of radius rad - 1 units of 2^sh around the unit of c
         int K[3];
@@ -391,13 +409,24 @@ __device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned ch
         n += crossings;
         t = T;
         axis = e;
-        if (n >= max_steps) break;
+        if (n >= max_steps) return kMiss;
         if ((unsigned)c[0] >= (unsigned)w.dims[0] || (unsigned)c[1] >= (unsigned)w.dims[1] ||
             (unsigned)c[2] >= (unsigned)w.dims[2])
-            break;
+            return kMiss;
         state = 0;
+        return kMore;
     }
-    return false;
+};
+
+template <bool MAT>
+__device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned char* cdist, const PRay& r,
+                                           int max_steps, TraceHit& h) {
+    Walker wk;
+    if (!wk.start(w, r.o, r.d, max_steps)) return false;
+    int s;
+    while ((s = wk.step<MAT>(w, cdist, h)) == Walker::kMore) {
+    }
+    return s == Walker::kHit;
 }
 
 }  // namespace vt

@@ -1,0 +1,139 @@
+// tune.cu -- launch-configuration autotuner of the render kernels.
+//
+// The candidates are the warp-tile shapes (8x4, 16x2, 32x1 pixels) and
+// register budgets of the one-thread-per-pixel kernel, and the refill batch of
+// the persistent pixel-queue kernel.  All produce identical records; the tuner
+// times each on the caller's frame and keeps the fastest.  Choices can be
+// cached in a small text file, one line per key:
+//     <gpu name>|<X>x<Y>x<Z>|<W>x<H>|<rays>|<shade> <kernel> <tile w> <occupancy> <batch> <ms>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "vt_internal.h"
+
+namespace {
+
+bool valid(const vt_tuning& t) {
+    if (t.kernel == VT_KERNEL_TILE)
+        return (t.warp_tile_w == 8 || t.warp_tile_w == 16 || t.warp_tile_w == 32) && (t.occupancy == 0 || t.occupancy == 1);
+    if (t.kernel == VT_KERNEL_QUEUE) return t.batch >= 1 && t.batch <= 32;
+    return false;
+}
+
+std::string cache_key(const vt_ctx* ctx, const vt_world* w, const vt_camera* cam, const vt_params* p) {
+    std::ostringstream k;
+    std::string name = ctx->name;
+    for (char& ch : name)
+        if (ch == ' ' || ch == '|') ch = '_';
+    k << name << '|' << w->dims[0] << 'x' << w->dims[1] << 'x' << w->dims[2] << '|' << cam->width << 'x'
+      << cam->height << '|' << (p->rays | VT_RAYS_PRIMARY) << '|' << p->shade;
+    return k.str();
+}
+
+bool cache_lookup(const char* path, const std::string& key, vt_tuning* t, float* ms) {
+    std::ifstream in(path);
+    std::string line;
+    bool found = false;
+    while (std::getline(in, line)) {
+        std::istringstream ls(line);
+        std::string k;
+        vt_tuning c;
+        float m;
+        if (ls >> k >> c.kernel >> c.warp_tile_w >> c.occupancy >> c.batch >> m && k == key && valid(c)) {
+            *t = c;
+            *ms = m;
+            found = true;  // the last record of a key wins
+        }
+    }
+    return found;
+}
+
+void cache_store(const char* path, const std::string& key, const vt_tuning& t, float ms) {
+    std::ofstream out(path, std::ios::app);
+    out << key << ' ' << t.kernel << ' ' << t.warp_tile_w << ' ' << t.occupancy << ' ' << t.batch << ' ' << ms << '\n';
+}
+
+}  // namespace
+
+using namespace vt;
+
+extern "C" {
+
+vt_status vt_set_tuning(vt_ctx* ctx, const vt_tuning* t) {
+    if (!ctx) return VT_ERR_ARG;
+    if (!t || !valid(*t)) return fail(ctx, VT_ERR_ARG, "invalid tuning");
+    ctx->tuning = *t;
+    return VT_OK;
+}
+
+vt_status vt_get_tuning(vt_ctx* ctx, vt_tuning* t) {
+    if (!ctx || !t) return VT_ERR_ARG;
+    *t = ctx->tuning;
+    return VT_OK;
+}
+
+vt_status vt_autotune(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* params, int32_t reps,
+                      const char* cache_path, vt_tuning* best, float* best_ms) {
+    if (!ctx) return VT_ERR_ARG;
+    if (!world || !cam || !params) return fail(ctx, VT_ERR_ARG, "null world, camera or params");
+    if (reps < 1 || reps > 10000) return fail(ctx, VT_ERR_ARG, "reps must be in [1, 10000]");
+    const std::string key = cache_key(ctx, world, cam, params);
+    vt_tuning found;
+    float found_ms = 0.0f;
+    if (cache_path && cache_lookup(cache_path, key, &found, &found_ms)) {
+        ctx->tuning = found;
+        if (best) *best = found;
+        if (best_ms) *best_ms = found_ms;
+        return VT_OK;
+    }
+    std::vector<vt_tuning> cands;
+    for (int tw : {8, 16, 32})
+        for (int occ : {0, 1}) cands.push_back(vt_tuning{VT_KERNEL_TILE, tw, occ, 16});
+    for (int b : {8, 16, 24}) cands.push_back(vt_tuning{VT_KERNEL_QUEUE, 8, 0, b});
+
+    const size_t bytes = (size_t)cam->width * cam->height * sizeof(vt_hit);
+    void* d_out = nullptr;
+    vt_status s = ctx_scratch(ctx, bytes, &d_out);
+    if (s) return s;
+    cudaEvent_t e0, e1;
+    VT_CUDA(ctx, cudaEventCreate(&e0));
+    VT_CUDA(ctx, cudaEventCreate(&e1));
+    const vt_tuning saved = ctx->tuning;
+    vt_tuning win = saved;
+    float win_ms = 0.0f;
+    bool have = false;
+    for (const vt_tuning& c : cands) {
+        ctx->tuning = c;
+        for (int i = 0; i < 2 && !s; ++i) s = vt_render(ctx, world, cam, params, (vt_hit*)d_out, ctx->stream);
+        if (!s) s = check_cuda(ctx, cudaEventRecord(e0, ctx->stream), "cudaEventRecord");
+        for (int i = 0; i < reps && !s; ++i) s = vt_render(ctx, world, cam, params, (vt_hit*)d_out, ctx->stream);
+        if (!s) s = check_cuda(ctx, cudaEventRecord(e1, ctx->stream), "cudaEventRecord");
+        if (!s) s = check_cuda(ctx, cudaEventSynchronize(e1), "cudaEventSynchronize");
+        float ms = 0.0f;
+        if (!s) s = check_cuda(ctx, cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        if (s) break;
+        ms /= (float)reps;
+        if (!have || ms < win_ms) {
+            win = c;
+            win_ms = ms;
+            have = true;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s) {
+        ctx->tuning = saved;
+        return s;
+    }
+    ctx->tuning = win;
+    if (cache_path) cache_store(cache_path, key, win, win_ms);
+    if (best) *best = win;
+    if (best_ms) *best_ms = win_ms;
+    return VT_OK;
+}
+
+}  // extern "C"

@@ -54,7 +54,15 @@ struct vt_ctx {
     cudaStream_t stream = nullptr;               // stream of the *_host entry points
     void* d_scratch = nullptr;                   // output staging of the *_host entry points
     size_t scratch_bytes = 0;
+    unsigned* d_work = nullptr;                  // ring of pixel-queue counters of the persistent kernels
+    unsigned work_slot = 0;
+    int persist_blocks = 0;                      // resident blocks per SM of the persistent render kernel
+    vt_tuning tuning = {VT_KERNEL_TILE, 8, 1, 16};
 };
+
+namespace vt {
+constexpr int kWorkSlots = 256;
+}
 
 struct vt_world {
     vt_ctx* ctx = nullptr;

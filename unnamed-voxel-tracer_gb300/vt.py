@@ -33,6 +33,7 @@ STATUS_NAMES = {0: "VT_OK", 1: "VT_ERR_ARG", 2: "VT_ERR_OOM", 3: "VT_ERR_CUDA", 
 RAYS_PRIMARY, RAYS_SHADOW, RAYS_BOUNCE = 1, 2, 4
 SHADE_NONE, SHADE_REFERENCE, SHADE_LAMBERT = 0, 1, 2
 FLAG_CROSSHAIR, FLAG_VIGNETTE, FLAG_CHECKED = 1, 2, 4
+KERNEL_TILE, KERNEL_QUEUE = 0, 1
 HIT_PRIMARY, HIT_SHADOWED, HIT_BOUNCE = 1, 2, 4
 
 
@@ -52,6 +53,13 @@ class Stats_t(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "primary_rays", "primary_hits", "shadow_rays", "shadow_hits", "bounce_rays", "bounce_hits",
         "mask_words", "coarse_words", "material_bytes", "record_bytes", "steps", "iterations")]
+
+    def as_dict(self) -> dict:
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+class Tuning_t(C.Structure):
+    _fields_ = [("kernel", C.c_int32), ("warp_tile_w", C.c_int32), ("occupancy", C.c_int32), ("batch", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -114,6 +122,10 @@ _SIGNATURES = {
     "vt_render_host": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), _P]),
     "vt_render_stats": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), C.POINTER(Stats_t), _P]),
     "vt_trace_rays": (_S, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, _P]),
+    "vt_set_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
+    "vt_get_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
+    "vt_autotune": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), C.c_int32, C.c_char_p,
+                         C.POINTER(Tuning_t), C.POINTER(C.c_float)]),
     "vt_gen_desc_init": (None, [C.POINTER(GenDesc_t), C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64]),
     "vt_gen_world": (_S, [C.POINTER(GenDesc_t), _P, C.c_size_t, C.c_int32]),
     "vt_gen_height": (C.c_int32, [C.POINTER(GenDesc_t), C.c_int32, C.c_int32]),
@@ -188,6 +200,24 @@ class Context:
 
     def sync(self, stream=None) -> None:
         self.check(self.lib.vt_sync(self.handle, stream))
+
+    def set_tuning(self, kernel: int = KERNEL_TILE, warp_tile_w: int = 8, occupancy: int = 0,
+                   batch: int = 16) -> None:
+        t = Tuning_t(kernel, warp_tile_w, occupancy, batch)
+        self.check(self.lib.vt_set_tuning(self.handle, C.byref(t)))
+
+    def get_tuning(self) -> dict:
+        t = Tuning_t()
+        self.check(self.lib.vt_get_tuning(self.handle, C.byref(t)))
+        return t.as_dict()
+
+    def autotune(self, world: "World", cam, params, reps: int = 5, cache_path: str | None = None):
+        """Times every launch configuration on this frame and keeps the fastest."""
+        t = Tuning_t()
+        ms = C.c_float()
+        self.check(self.lib.vt_autotune(self.handle, world.handle, C.byref(cam), C.byref(params), reps,
+                                        cache_path.encode() if cache_path else None, C.byref(t), C.byref(ms)))
+        return t.as_dict(), float(ms.value)
 
     def device_info(self) -> tuple[str, int]:
         buf = C.create_string_buffer(256)
