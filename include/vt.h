@@ -197,6 +197,24 @@ vt_status vt_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
 vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
                          const vt_params* params, vt_hit* h_out);
 
+/* No counterpart in the reference.  vt_render_host for callers that cannot
+ * allocate device memory: hosts that hand out all device memory through
+ * their own allocator and forbid other allocations, and real-time frame loops
+ * that must not call cudaMalloc once running (it can synchronize the device).
+ * vt_render_host stages the records in a buffer the context allocates on
+ * first use; this call stages them in a fixed device array compiled into the
+ * library (VT_STATIC_MAX_PIXELS records, 4 MiB, held by every GPU that loads
+ * the library until exit) and allocates nothing.
+ *   - Frames larger than VT_STATIC_MAX_PIXELS pixels are rejected (VT_ERR_ARG).
+ *   - The first call on a device looks the array's device address up
+ *     (cudaGetSymbolAddress, with that device current); make that first call
+ *     before any stream capture.
+ *   - All calls share the one array: calls whose work overlaps on the GPU
+ *     (several host threads, several contexts) race on it. */
+#define VT_STATIC_MAX_PIXELS 262144
+vt_status vt_render_host_static(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
+                                const vt_params* params, vt_hit* h_out);
+
 /* Counters of one render, from an instrumented kernel variant.  The byte
  * counts are algorithmic: 8 per brick word and per coarse word consulted,
  * 1 per material byte read on a hit, 16 per record stored. */

@@ -389,7 +389,7 @@ vt_status check_frame_args(vt_ctx* ctx, const vt_world* world, const vt_camera* 
     return VT_OK;
 }
 
-static vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p,
+vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p,
                                uint4* d_out, cudaStream_t stream, bool stats) {
     const FrameParams f = make_frame(cam, p);
     const WorldView w = world->view();

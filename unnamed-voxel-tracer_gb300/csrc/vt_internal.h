@@ -109,6 +109,12 @@ vt_status check_cuda(vt_ctx* ctx, cudaError_t err, const char* what);
 vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out);
 // Rebuilds the empty-space distances of a world on `st`.
 vt_status rebuild_distances(vt_world* w, cudaStream_t st);
+// Argument checks shared by the render entry points.
+vt_status check_frame_args(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p);
+// Queues one frame (render kernel, distances rebuilt first if stale) writing
+// width*height records to d_out on `stream`.
+vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p, uint4* d_out,
+                        cudaStream_t stream, bool stats);
 }  // namespace vt
 
 #define VT_CUDA(ctx, call)                                                      \

@@ -120,6 +120,7 @@ _SIGNATURES = {
     "vt_params_default": (None, [C.POINTER(Params_t)]),
     "vt_render": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), _P, _P]),
     "vt_render_host": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), _P]),
+    "vt_render_host_static": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), _P]),
     "vt_render_stats": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), C.POINTER(Stats_t), _P]),
     "vt_trace_rays": (_S, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, _P]),
     "vt_set_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
@@ -366,6 +367,19 @@ def render_host(ctx: Context, world: World, cam: Camera_t, params: Params_t, out
         out = np.zeros(cam.width * cam.height, dtype=HIT_DTYPE)
     assert out.dtype == HIT_DTYPE and out.size >= cam.width * cam.height
     ctx.check(ctx.lib.vt_render_host(ctx.handle, world.handle, C.byref(cam), C.byref(params), _ptr(out)))
+    return out
+
+
+STATIC_MAX_PIXELS = 262144
+
+
+def render_host_static(ctx: Context, world: World, cam: Camera_t, params: Params_t, out: np.ndarray | None = None):
+    """render_host without any device allocation (records staged in the
+    library's fixed device array; frames of at most STATIC_MAX_PIXELS)."""
+    if out is None:
+        out = np.zeros(cam.width * cam.height, dtype=HIT_DTYPE)
+    assert out.dtype == HIT_DTYPE and out.size >= cam.width * cam.height
+    ctx.check(ctx.lib.vt_render_host_static(ctx.handle, world.handle, C.byref(cam), C.byref(params), _ptr(out)))
     return out
 
 
