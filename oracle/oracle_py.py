@@ -68,6 +68,9 @@ def load() -> C.CDLL:
         lib.vto_cosf.restype = C.c_float
         lib.vto_tracemap.argtypes = [C.POINTER(VtoRefWorld_t), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                      C.c_int32, C.POINTER(VtoRefHit_t)]
+        lib.vto_primary_r.argtypes = [C.POINTER(VtoRefWorld_t), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                      C.c_float, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                      C.POINTER(C.c_float), C.POINTER(VtoRefHit_t)]
         _lib = lib
     return _lib
 
@@ -134,3 +137,40 @@ def tracemap(world: OracleRefWorld, o, d, max_steps: int) -> VtoRefHit_t:
     h = VtoRefHit_t()
     load().vto_tracemap(C.byref(world.w), (C.c_float * 3)(*o), (C.c_float * 3)(*d), max_steps, C.byref(h))
     return h
+
+
+def primary_r(world: OracleRefWorld, cam_pos, view, fov: float, px: int, py: int, width: int, height: int,
+              max_steps: int = 192):
+    """The reference's primary ray (primary.comp.glsl:31-43): (direction, hit)."""
+    h = VtoRefHit_t()
+    d = (C.c_float * 3)()
+    load().vto_primary_r(C.byref(world.w), (C.c_float * 4)(*cam_pos), (C.c_float * 16)(*view), fov, px, py, width,
+                         height, max_steps, d, C.byref(h))
+    return [d[0], d[1], d[2]], h
+
+
+# ---- the reference's own shader code compiled as C++ (oracle/_ref/libref.so),
+# available where the reference sources are (built by oracle/build_ref.py)
+REF_LIB = HERE / "_ref" / "libref.so"
+_ref = None
+
+
+def load_ref():
+    """The compiled reference shaders, or None where they cannot be built."""
+    global _ref
+    if _ref is None:
+        spec = importlib.util.spec_from_file_location("vt_ref_build", HERE / "build_ref.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        if mod.build_if_available() is None or not REF_LIB.exists():
+            return None
+        lib = C.CDLL(str(REF_LIB))
+        P, F = C.c_void_p, C.POINTER(C.c_float)
+        lib.ref_set_world.argtypes = [P, P, P]
+        lib.ref_trace_map.argtypes = [F, F, C.c_int32, C.POINTER(C.c_uint32), F, F]
+        lib.ref_trace_entities.argtypes = [F, F, C.c_float, C.POINTER(C.c_uint32), F, F]
+        lib.ref_sky.argtypes = [F, F, F]
+        lib.ref_primary.argtypes = [F, F, C.c_float, C.c_int32, C.c_int32, C.c_int32, C.c_int32, F,
+                                    C.POINTER(C.c_uint32), F, F]
+        _ref = lib
+    return _ref

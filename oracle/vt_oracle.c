@@ -645,3 +645,40 @@ void vto_tracemap(const vto_refworld* w, const float o[3], const float din[3], i
     out->hit_pos[0] = out->hit_pos[1] = out->hit_pos[2] = -1.0f;
     out->normal[0] = out->normal[1] = out->normal[2] = 0.0f;
 }
+
+/* primary.comp.glsl:31-43 restated: uv, fov scale, C_view * vec4(uv, 1, 1)
+ * with the matrix read column-major, 4-D normalisation, intersectAABB
+ * (map.glsl:21-29) against [0, 512]^3, start at o + d * max(tNear, 0) - 0.001. */
+static float fmin_g(float a, float b) { return b < a ? b : a; }
+static float fmax_g(float a, float b) { return a < b ? b : a; }
+
+void vto_primary_r(const vto_refworld* w, const float cam_pos[4], const float view[16], float fov, int32_t px,
+                   int32_t py, int32_t width, int32_t height, int32_t max_steps, float dir_out[3], vto_refhit* out) {
+    float ux = (float)px / (float)width * 2.0f - 1.0f;
+    float uy = (float)py / (float)height * 2.0f - 1.0f;
+    uy *= (float)height / (float)width;
+    const float th = tanf(fov / 2.0f);
+    ux *= th;
+    uy *= th;
+    const float v[4] = {ux, uy, 1.0f, 1.0f};
+    float q[4];
+    for (int i = 0; i < 4; ++i)
+        q[i] = ((view[0 * 4 + i] * v[0] + view[1 * 4 + i] * v[1]) + view[2 * 4 + i] * v[2]) + view[3 * 4 + i] * v[3];
+    const float len = sqrtf(((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]) + q[3] * q[3]);
+    float d[3], o[3], t1[3];
+    for (int i = 0; i < 3; ++i) {
+        d[i] = q[i] / len;
+        o[i] = cam_pos[i];
+    }
+    for (int i = 0; i < 3; ++i) {
+        const float tmin = (0.0f - o[i]) / d[i];
+        const float tmax = (512.0f - o[i]) / d[i];
+        t1[i] = fmin_g(tmin, tmax);
+    }
+    const float tnear = fmax_g(fmax_g(t1[0], t1[1]), t1[2]);
+    const float s = fmax_g(tnear, 0.0f);
+    float start[3];
+    for (int i = 0; i < 3; ++i) start[i] = (o[i] + d[i] * s) - 0.001f;
+    for (int i = 0; i < 3; ++i) dir_out[i] = d[i];
+    vto_tracemap(w, start, d, max_steps, out);
+}

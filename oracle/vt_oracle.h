@@ -97,6 +97,13 @@ typedef struct {
 
 void vto_tracemap(const vto_refworld* w, const float o[3], const float d[3], int32_t max_steps, vto_refhit* out);
 
+/* The reference's primary ray for pixel (px, py) of a W x H image
+ * (primary.comp.glsl:31-43): camera = C_position, C_view (16 floats as the
+ * host stores them, read column-major), fov; the ray is clipped to the 512^3
+ * map box and traced with traceMap(..., max_steps). */
+void vto_primary_r(const vto_refworld* w, const float cam_pos[4], const float view[16], float fov, int32_t px,
+                   int32_t py, int32_t width, int32_t height, int32_t max_steps, float dir_out[3], vto_refhit* out);
+
 #ifdef __cplusplus
 }
 #endif
