@@ -235,6 +235,41 @@ typedef struct {
 vt_status vt_render_stats(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
                           const vt_params* params, vt_stats* out, vt_stream stream);
 
+/* ------------------------------------------------------- shading adjoint
+ * No counterpart in the reference (its shading is fixed-function,
+ * blit.fragment.glsl:31).  Lambert + shadowed sun over the primary hits of a
+ * frame, with the hit set held fixed (the discrete traversal is never
+ * relaxed):
+ *     c = palette[m] * albedo[v] * (ambient + diffuse * max(0, n . s/|s|) * V)
+ * m, v, n from the primary hit record, V = 1 unless the shadow ray from the
+ * hit toward s (traced exactly as vt_render traces it) hits a voxel; c = 0 on
+ * a miss.  Loss L = sum over pixels and channels of (c - target)^2. */
+typedef struct {
+    const float* d_palette;  /* 256 x 3 FP32 RGB */
+    const float* d_albedo;   /* X*Y*Z FP32 per-voxel scale (index x + X*(y + Y*z)), or NULL for 1 */
+    float sun[3];            /* sun direction (any length) */
+    float ambient;
+    float diffuse;
+    int32_t shadow_max_steps;
+} vt_shade_inputs;
+
+/* Forward shading: d_rgb gets width*height*3 floats.  d_hits are the records
+ * of vt_render for the same camera.  With d_vis_in != NULL the shadow term is
+ * read from it (one byte per pixel, 1 = lit) instead of traced; d_vis_out,
+ * if not NULL, receives the traced one. */
+vt_status vt_shade_forward(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_hit* d_hits,
+                           const vt_shade_inputs* in, const uint8_t* d_vis_in, uint8_t* d_vis_out, float* d_rgb,
+                           vt_stream stream);
+/* Fused forward + backward of the loss: recomputes the shading (shadow rays
+ * traced again, not stored), adds the loss to *d_loss and the gradients to
+ * d_grad_palette (256 x 3), d_grad_albedo (X*Y*Z, may be NULL) and
+ * d_grad_sun (3).  The caller owns and zeroes these accumulators.  Gradients
+ * are accumulated with float atomics, so their last bits depend on the order
+ * in which blocks finish. */
+vt_status vt_shade_backward(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_hit* d_hits,
+                            const vt_shade_inputs* in, const float* d_target, float* d_loss, float* d_grad_palette,
+                            float* d_grad_albedo, float* d_grad_sun, vt_stream stream);
+
 /* ------------------------------------------------------------------ tuning
  * Launch configuration of the render kernels (no counterpart in the
  * reference, whose dispatch shape is fixed at 32x32 groups, game.zig:241-248).

@@ -71,6 +71,10 @@ def load() -> C.CDLL:
         lib.vto_primary_r.argtypes = [C.POINTER(VtoRefWorld_t), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                       C.c_float, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                       C.POINTER(C.c_float), C.POINTER(VtoRefHit_t)]
+        lib.vto_shade_grad_f64.argtypes = [C.POINTER(VtoWorld_t), C.POINTER(vt.Camera_t), P, P, P,
+                                           C.POINTER(C.c_double), C.c_double, C.c_double, C.c_int32, P, P, P, P,
+                                           P, P, P, C.POINTER(C.c_double)]
+        lib.vto_shade_grad_f64.restype = C.c_int32
         _lib = lib
     return _lib
 
@@ -137,6 +141,35 @@ def tracemap(world: OracleRefWorld, o, d, max_steps: int) -> VtoRefHit_t:
     h = VtoRefHit_t()
     load().vto_tracemap(C.byref(world.w), (C.c_float * 3)(*o), (C.c_float * 3)(*d), max_steps, C.byref(h))
     return h
+
+
+def shade_grad_f64(world: OracleWorld, cam, hits: np.ndarray, palette, albedo, sun, ambient: float, diffuse: float,
+                   shadow_max_steps: int, target: np.ndarray | None = None, vis_in: np.ndarray | None = None) -> dict:
+    """FP64 Lambert shading of one view and the exact gradient of
+    L = sum (c - target)^2 over the fixed hit set (records from render)."""
+    n = cam.width * cam.height
+    X, Y, Z = world.dims
+    pal = np.ascontiguousarray(palette, np.float64).reshape(768)
+    alb = None if albedo is None else np.ascontiguousarray(albedo, np.float64).reshape(-1)
+    hits = np.ascontiguousarray(hits)
+    rgb = np.zeros(n * 3, np.float64)
+    vis = np.zeros(n, np.uint8)
+    loss = np.zeros(1, np.float64)
+    g_pal = np.zeros(768, np.float64)
+    g_alb = np.zeros(X * Y * Z, np.float64) if alb is not None else None
+    g_sun = (C.c_double * 3)()
+    tgt = None if target is None else np.ascontiguousarray(target, np.float32).reshape(-1)
+    vin = None if vis_in is None else np.ascontiguousarray(vis_in, np.uint8).reshape(-1)
+    rc = load().vto_shade_grad_f64(
+        C.byref(world.w), C.byref(cam), hits.ctypes.data, pal.ctypes.data,
+        alb.ctypes.data if alb is not None else None, (C.c_double * 3)(*sun), ambient, diffuse, shadow_max_steps,
+        tgt.ctypes.data if tgt is not None else None, vin.ctypes.data if vin is not None else None, vis.ctypes.data,
+        rgb.ctypes.data, loss.ctypes.data, g_pal.ctypes.data, g_alb.ctypes.data if g_alb is not None else None,
+        g_sun)
+    if rc != 0:
+        raise ValueError("bad shading arguments")
+    return {"rgb": rgb.reshape(n, 3), "vis": vis, "loss": float(loss[0]), "palette": g_pal.reshape(256, 3),
+            "albedo": g_alb, "sun": np.array(list(g_sun))}
 
 
 def primary_r(world: OracleRefWorld, cam_pos, view, fov: float, px: int, py: int, width: int, height: int,

@@ -547,6 +547,76 @@ void vto_trace_rays(const vto_world* w, const float* origins, const float* dirs,
 }
 
 /* ======================================================================
+ * Shading adjoint reference (FP64 arithmetic over the float traversal's
+ * discrete hit and shadow sets).
+ * ====================================================================== */
+int32_t vto_shade_grad_f64(const vto_world* w, const vt_camera* cam, const vt_hit* hits, const double* pal,
+                           const double* alb, const double sun[3], double ka, double kd, int32_t shadow_max_steps,
+                           const float* target, const uint8_t* vis_in, uint8_t* vis_out, double* rgb, double* loss,
+                           double* g_pal, double* g_alb, double g_sun[3]) {
+    const double len = sqrt(sun[0] * sun[0] + sun[1] * sun[1] + sun[2] * sun[2]);
+    if (!(len > 0.0)) return 1;
+    const double sn[3] = {sun[0] / len, sun[1] / len, sun[2] / len};
+    const float sunf[3] = {(float)sun[0], (float)sun[1], (float)sun[2]};
+    const int W = cam->width, H = cam->height;
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            const size_t p = (size_t)py * W + px;
+            const vt_hit* h = hits + p;
+            double c[3] = {0.0, 0.0, 0.0};
+            int lit = 0;
+            const int hit = (h->flags & VT_HIT_PRIMARY) != 0;
+            double shade = 0.0, albv = 1.0, ndl = 0.0;
+            double nrm[3] = {0.0, 0.0, 0.0};
+            const int m = h->material;
+            if (hit) {
+                const int axis = h->face >> 1;
+                const int pos = (h->face & 1) == 0;
+                float o[3], d[3];
+                primary_ray(cam, px, py, o, d);
+                pray r;
+                pray_init(&r, o, d);
+                float so[3], nf[3] = {0.0f, 0.0f, 0.0f};
+                nf[axis] = pos ? -1.0f : 1.0f;
+                nrm[axis] = nf[axis];
+                for (int j = 0; j < 3; ++j) so[j] = fmaf(r.d[j], h->t, o[j]);
+                so[axis] = so[axis] + nf[axis] * 0.001f;
+                if (vis_in) {
+                    lit = vis_in[p] != 0;
+                } else {
+                    vto_trace ts;
+                    vto_trace_p(w, so, sunf, shadow_max_steps, &ts);
+                    lit = !ts.hit;
+                }
+                ndl = nrm[0] * sn[0] + nrm[1] * sn[1] + nrm[2] * sn[2];
+                shade = ka + kd * (ndl > 0.0 ? ndl : 0.0) * (lit ? 1.0 : 0.0);
+                albv = alb ? alb[h->voxel] : 1.0;
+                for (int k = 0; k < 3; ++k) c[k] = pal[3 * m + k] * albv * shade;
+            }
+            if (vis_out) vis_out[p] = (uint8_t)(hit && lit);
+            if (rgb)
+                for (int k = 0; k < 3; ++k) rgb[3 * p + k] = c[k];
+            if (!target) continue;
+            double g[3], gb = 0.0, ga = 0.0;
+            for (int k = 0; k < 3; ++k) {
+                const double diff = c[k] - (double)target[3 * p + k];
+                g[k] = 2.0 * diff;
+                if (loss) *loss += diff * diff;
+            }
+            if (!hit) continue;
+            for (int k = 0; k < 3; ++k) {
+                if (g_pal) g_pal[3 * m + k] += g[k] * albv * shade;
+                ga += g[k] * pal[3 * m + k] * shade;
+                gb += g[k] * pal[3 * m + k] * albv;
+            }
+            if (g_alb) g_alb[h->voxel] += ga;
+            if (g_sun && lit && ndl > 0.0)
+                for (int k = 0; k < 3; ++k) g_sun[k] += gb * kd * (nrm[k] - ndl * sn[k]) / len;
+        }
+    return 0;
+}
+
+/* ======================================================================
  * Mode R: traceMap (map.glsl:83-168) restated operation by operation.
  * GLSL float->int conversions truncate toward zero; float->uint saturates
  * negative values to 0 (as the GPU's conversion does).

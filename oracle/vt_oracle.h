@@ -76,6 +76,17 @@ int32_t vto_render_sampled(const vto_world* w, const uint32_t* palette, const vt
 void vto_trace_rays(const vto_world* w, const float* origins, const float* dirs, int32_t n,
                     int32_t max_steps, vt_hit* out);
 
+/* Lambert + shadowed-sun shading of one view and its exact gradient, in FP64,
+ * over the primary hit records `hits` (from vto_render with primary rays):
+ *     c = pal[m] * alb[v] * (ka + kd * max(0, n . s/|s|) * V),  L = sum (c - target)^2
+ * V is read from vis_in (1 = lit) when not NULL, else traced from the hit with
+ * the mode-P traversal (shadow origin as in the render path); vis_out, rgb,
+ * g_pal (768), g_alb (X*Y*Z) may be NULL.  Gradients are added to the outputs. */
+int32_t vto_shade_grad_f64(const vto_world* w, const vt_camera* cam, const vt_hit* hits, const double* pal,
+                           const double* alb, const double sun[3], double ka, double kd, int32_t shadow_max_steps,
+                           const float* target, const uint8_t* vis_in, uint8_t* vis_out, double* rgb, double* loss,
+                           double* g_pal, double* g_alb, double g_sun[3]);
+
 /* The deterministic sine/cosine used for bounce directions. */
 float vto_sinf(float x);
 float vto_cosf(float x);

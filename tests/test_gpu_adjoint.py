@@ -1,0 +1,132 @@
+"""Shading adjoint on the GPU (vt_shade_forward / vt_shade_backward) against
+the FP64 CPU gradient over the same hit and shadow sets, and against central
+finite differences of the GPU forward image (h = 1e-3, shadow set held fixed).
+
+Tolerance: gradients within 1e-4 of the FP64 reference, relative to the
+largest component of each parameter group; forward colours within 1e-6."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def scene(vt, ctx, oracle):
+    d = vt.gen_desc((256, 256, 256), seed=4, trees=50)
+    mats = vt.gen_world(d)
+    rng = np.random.default_rng(4)
+    occ = mats > 0
+    mats[occ] = rng.integers(1, 40, occ.sum()).astype(np.uint8)
+    w = vt.World(ctx, (256, 256, 256))
+    w.upload_dense(mats)
+    cams = [vt.gen_camera(d, v, 128, 96) for v in range(2)]
+    prim = vt.default_params(rays=vt.RAYS_PRIMARY, shade=vt.SHADE_NONE)
+    hits = []
+    for cam in cams:
+        hb = ctx.alloc(cam.width * cam.height * 16)
+        vt.render(ctx, w, cam, prim, hb)
+        hits.append(hb)
+    ctx.sync()
+    pal = rng.uniform(0.05, 0.95, (256, 3)).astype(np.float32)
+    alb = rng.uniform(0.5, 1.5, mats.size).astype(np.float32)
+    sun = np.array(vt.gen_sun(9), np.float32)
+    targets = [rng.uniform(0, 1, (c.width * c.height, 3)).astype(np.float32) for c in cams]
+    sh = vt.Shading(ctx, w, pal, alb, sun)
+    yield dict(mats=mats, world=w, cams=cams, hits=hits, pal=pal, alb=alb, sun=sun, targets=targets, sh=sh,
+               ow=oracle.OracleWorld(mats))
+    sh.close()
+    for hb in hits:
+        hb.free()
+    w.close()
+
+
+def records(vt, hb, cam):
+    out = np.zeros(cam.width * cam.height, vt.HIT_DTYPE)
+    return hb.download(out)
+
+
+def test_forward_matches_fp64(vt, ctx, oracle, scene):
+    s = scene
+    for cam, hb in zip(s["cams"], s["hits"]):
+        rgb = ctx.alloc(cam.width * cam.height * 12)
+        vis = ctx.alloc(cam.width * cam.height)
+        s["sh"].forward(cam, hb, rgb, vis_out=vis)
+        ctx.sync()
+        got = rgb.download(np.zeros((cam.width * cam.height, 3), np.float32))
+        gvis = vis.download(np.zeros(cam.width * cam.height, np.uint8))
+        ref = oracle.shade_grad_f64(s["ow"], cam, records(vt, hb, cam), s["pal"], s["alb"], s["sun"], 0.2, 0.8, 512)
+        assert np.array_equal(gvis, ref["vis"])
+        assert np.abs(got - ref["rgb"]).max() <= 1e-6
+        assert gvis.sum() > 100 and (gvis == 0).sum() > 100
+        rgb.free()
+        vis.free()
+
+
+def test_backward_matches_fp64_gradient(vt, ctx, oracle, scene):
+    s = scene
+    sh = s["sh"]
+    sh.zero_grad()
+    ref_loss, ref_pal, ref_alb, ref_sun = 0.0, np.zeros((256, 3)), np.zeros(s["mats"].size), np.zeros(3)
+    for cam, hb, tgt in zip(s["cams"], s["hits"], s["targets"]):
+        dt = ctx.alloc(tgt.nbytes)
+        dt.upload(tgt)
+        sh.backward(cam, hb, dt)
+        ctx.sync()
+        dt.free()
+        r = oracle.shade_grad_f64(s["ow"], cam, records(vt, hb, cam), s["pal"], s["alb"], s["sun"], 0.2, 0.8, 512,
+                                  tgt)
+        ref_loss += r["loss"]
+        ref_pal += r["palette"]
+        ref_alb += r["albedo"]
+        ref_sun += r["sun"]
+    g = sh.grads()
+    assert g["loss"] == pytest.approx(ref_loss, rel=REL)
+    assert np.abs(g["palette"] - ref_pal).max() <= REL * np.abs(ref_pal).max()
+    assert np.abs(g["albedo"] - ref_alb).max() <= REL * np.abs(ref_alb).max()
+    assert np.abs(g["sun"] - ref_sun).max() <= REL * np.abs(ref_sun).max()
+    assert (np.abs(ref_pal).sum(1) > 0).sum() >= 20 and np.count_nonzero(ref_alb) > 1000
+
+
+def test_backward_matches_finite_differences(vt, ctx, scene):
+    """(L(p + h) - L(p - h)) / 2h from GPU forward images, shadow set fixed."""
+    s = scene
+    cam, hb, tgt = s["cams"][0], s["hits"][0], s["targets"][0]
+    n = cam.width * cam.height
+    rgb, vis = ctx.alloc(n * 12), ctx.alloc(n)
+    sh = s["sh"]
+    sh.forward(cam, hb, rgb, vis_out=vis)
+
+    def loss(pal, alb, sun):
+        sh.set_params(pal, alb, sun)
+        sh.forward(cam, hb, rgb, vis_in=vis)
+        ctx.sync()
+        c = rgb.download(np.zeros((n, 3), np.float32)).astype(np.float64)
+        return float(((c - tgt.astype(np.float64)) ** 2).sum())
+
+    sh.set_params(s["pal"], s["alb"], s["sun"])
+    sh.zero_grad()
+    dt = ctx.alloc(tgt.nbytes)
+    dt.upload(tgt)
+    sh.backward(cam, hb, dt)
+    g = sh.grads()
+    h = 1e-3
+    hits = records(vt, hb, cam)
+    mats_seen = np.unique(hits["material"][(hits["flags"] & 1) == 1])[:4]
+    for m in mats_seen:
+        for k in range(3):
+            p1, p2 = s["pal"].copy(), s["pal"].copy()
+            p1[m, k] += h
+            p2[m, k] -= h
+            fd = (loss(p1, s["alb"], s["sun"]) - loss(p2, s["alb"], s["sun"])) / (2 * h)
+            assert fd == pytest.approx(g["palette"][m, k], rel=2e-3, abs=2e-3 * np.abs(g["palette"]).max())
+    for k in range(3):
+        s1, s2 = s["sun"].copy(), s["sun"].copy()
+        s1[k] += h
+        s2[k] -= h
+        fd = (loss(s["pal"], s["alb"], s1) - loss(s["pal"], s["alb"], s2)) / (2 * h)
+        assert fd == pytest.approx(g["sun"][k], rel=2e-3, abs=2e-3 * np.abs(g["sun"]).max())
+    sh.set_params(s["pal"], s["alb"], s["sun"])
+    for b in (rgb, vis, dt):
+        b.free()

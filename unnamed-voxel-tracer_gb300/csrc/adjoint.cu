@@ -1,0 +1,285 @@
+// adjoint.cu -- differentiable Lambert shading over a fixed hit set.
+//
+//     c = palette[m] * albedo[v] * (ka + kd * max(0, n . s^) * V),  s^ = s / |s|
+//     L = sum (c - target)^2
+//     dL/dpalette[m]  = 2 (c - t) * albedo[v] * shade
+//     dL/dalbedo[v]   = sum_k 2 (c_k - t_k) * palette[m][k] * shade
+//     dL/ds           = (sum_k 2 (c_k - t_k) palette[m][k] albedo[v]) * kd * V * [n . s^ > 0]
+//                       * (n - (n . s^) s^) / |s|
+//
+// The primary hits (voxel, face, material, t) come from vt_render and are held
+// fixed; the shadow term V is recomputed here by tracing the shadow ray from
+// the hit exactly as the render kernel does (same origin arithmetic, same
+// traversal), instead of being stored between passes.  The backward kernel is
+// the forward kernel plus the loss and gradient epilogue, one thread per
+// pixel.  Gradients are summed per warp over lanes that share a material or a
+// voxel (__match_any_sync groups), per block in shared memory, then once per
+// block with global atomics.
+#include <cstring>
+
+#include "shade.cuh"
+#include "trace_p.cuh"
+
+namespace vt {
+
+namespace {
+
+constexpr int kAdjBlock = 256;
+constexpr size_t kMaxSharedDist = 48 * 1024;
+
+struct AdjArgs {
+    WorldView w;
+    FrameParams f;
+    const uint4* hits;
+    const float* pal;
+    const float* alb;
+    float sun[3], sun_n[3], inv_len;
+    float ka, kd;
+    int shadow_steps;
+    const unsigned char* vis_in;
+    unsigned char* vis_out;
+    float* rgb;
+    const float* target;
+    float* loss;
+    float* gpal;
+    float* galb;
+    float* gsun;
+};
+
+// Sum of v over the lanes of group g (every lane of g gets the same value,
+// summed in lane order).
+__device__ __forceinline__ float group_sum(unsigned g, float v) {
+    float s = 0.0f;
+    unsigned mm = g;
+    while (mm) {
+        const int l = __ffs(mm) - 1;
+        s += __shfl_sync(g, v, l);
+        mm &= mm - 1u;
+    }
+    return s;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+template <bool BWD, bool SMEM>
+__global__ void __launch_bounds__(kAdjBlock) k_shade(AdjArgs a) {
+    extern __shared__ float s_mem[];
+    float* s_gpal = s_mem;            // 768
+    float* s_acc = s_mem + 768;       // loss, sun x3
+    const unsigned char* cd = a.w.cdist;
+    if (BWD) {
+        for (int i = threadIdx.x; i < 772; i += blockDim.x) s_mem[i] = 0.0f;
+    }
+    if (SMEM) {
+        uint4* s_cd = reinterpret_cast<uint4*>(s_mem + 776);
+        const uint4* src = reinterpret_cast<const uint4*>(a.w.cdist);
+        for (unsigned i = threadIdx.x; i < (a.w.nchunks + 15u) / 16u; i += blockDim.x) s_cd[i] = __ldg(src + i);
+        cd = reinterpret_cast<const unsigned char*>(s_cd);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    const int py = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+    const bool inside = px < a.f.width && py < a.f.height;
+    const size_t p = inside ? (size_t)py * a.f.width + px : 0;
+
+    bool hit = false;
+    int m = 0;
+    unsigned v = 0;
+    float c[3] = {0.0f, 0.0f, 0.0f}, shade = 0.0f, albv = 1.0f, ndl_raw = 0.0f, nrm[3] = {0.0f, 0.0f, 0.0f};
+    bool lit = false;
+    if (inside) {
+        const uint4 rec = a.hits[p];
+        hit = ((rec.w >> 16) & VT_HIT_PRIMARY) != 0;
+        if (hit) {
+            v = rec.x;
+            const float t = __uint_as_float(rec.y);
+            const unsigned face = rec.w & 0xFFu;
+            m = (int)((rec.w >> 8) & 0xFFu);
+            const int axis = (int)(face >> 1);
+            const bool pos = (face & 1u) == 0u;
+            float o[3], d[3];
+            primary_ray(a.f, px, py, o, d);
+            PRay r;
+            pray_init(r, o, d);
+            float so[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                nrm[j] = (j == axis) ? (pos ? -1.0f : 1.0f) : 0.0f;
+                so[j] = __fmaf_rn(r.d[j], t, o[j]);
+                if (j == axis) so[j] = so[j] + nrm[j] * 0.001f;
+            }
+            if (a.vis_in) {
+                lit = a.vis_in[p] != 0;
+            } else {
+                PRay rs;
+                pray_init(rs, so, a.sun);
+                TraceHit hs;
+                lit = !trace_fast<false>(a.w, cd, rs, a.shadow_steps, hs);
+            }
+            ndl_raw = dot3(nrm, a.sun_n);
+            const float ndl = ndl_raw > 0.0f ? ndl_raw : 0.0f;
+            shade = a.ka + a.kd * ndl * (lit ? 1.0f : 0.0f);
+            albv = a.alb ? __ldg(a.alb + v) : 1.0f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) c[k] = (__ldg(a.pal + 3 * m + k) * albv) * shade;
+        }
+    }
+    if (!BWD) {
+        if (inside) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a.rgb[3 * p + k] = c[k];
+            if (a.vis_out) a.vis_out[p] = (unsigned char)(hit && lit ? 1 : 0);
+        }
+        return;
+    }
+
+    // ---- loss and gradients
+    float g[3] = {0.0f, 0.0f, 0.0f}, lossv = 0.0f;
+    if (inside) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float diff = c[k] - __ldg(a.target + 3 * p + k);
+            g[k] = 2.0f * diff;
+            lossv += diff * diff;
+        }
+    }
+    float gp[3] = {0.0f, 0.0f, 0.0f}, ga = 0.0f, gs[3] = {0.0f, 0.0f, 0.0f};
+    if (hit) {
+        float gb = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float pk = __ldg(a.pal + 3 * m + k);
+            gp[k] = g[k] * albv * shade;
+            ga += g[k] * pk * shade;
+            gb += g[k] * pk * albv;
+        }
+        if (lit && ndl_raw > 0.0f) {
+            const float coef = gb * a.kd * a.inv_len;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) gs[k] = coef * (nrm[k] - ndl_raw * a.sun_n[k]);
+        }
+    }
+    // palette: one shared-memory atomic per (warp, material)
+    {
+        const unsigned grp = __match_any_sync(0xFFFFFFFFu, hit ? m : -1);
+        const float s0 = group_sum(grp, gp[0]), s1 = group_sum(grp, gp[1]), s2 = group_sum(grp, gp[2]);
+        if (hit && lane == __ffs(grp) - 1) {
+            atomicAdd(s_gpal + 3 * m + 0, s0);
+            atomicAdd(s_gpal + 3 * m + 1, s1);
+            atomicAdd(s_gpal + 3 * m + 2, s2);
+        }
+    }
+    // albedo: one global atomic per (warp, voxel)
+    if (a.galb) {
+        const unsigned grp = __match_any_sync(0xFFFFFFFFu, hit ? v : 0xFFFFFFFFu);
+        const float s = group_sum(grp, ga);
+        if (hit && lane == __ffs(grp) - 1) atomicAdd(a.galb + v, s);
+    }
+    // loss and sun: warp sums, then shared memory
+    {
+        const float l = warp_sum(lossv), x = warp_sum(gs[0]), y = warp_sum(gs[1]), z = warp_sum(gs[2]);
+        if (lane == 0) {
+            atomicAdd(s_acc + 0, l);
+            atomicAdd(s_acc + 1, x);
+            atomicAdd(s_acc + 2, y);
+            atomicAdd(s_acc + 3, z);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 768; i += blockDim.x)
+        if (s_gpal[i] != 0.0f) atomicAdd(a.gpal + i, s_gpal[i]);
+    if (threadIdx.x == 0) {
+        atomicAdd(a.loss, s_acc[0]);
+        atomicAdd(a.gsun + 0, s_acc[1]);
+        atomicAdd(a.gsun + 1, s_acc[2]);
+        atomicAdd(a.gsun + 2, s_acc[3]);
+    }
+}
+
+vt_status launch_shade(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_hit* d_hits,
+                       const vt_shade_inputs* in, AdjArgs a, bool bwd, cudaStream_t st) {
+    if (!ctx) return VT_ERR_ARG;
+    if (!world || !cam || !d_hits || !in || !in->d_palette) return fail(ctx, VT_ERR_ARG, "null shading argument");
+    if (world->ctx != ctx) return fail(ctx, VT_ERR_ARG, "world belongs to another context");
+    if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
+        return fail(ctx, VT_ERR_ARG, "camera size out of range (1..32768)");
+    const float len2 = (in->sun[0] * in->sun[0] + in->sun[1] * in->sun[1]) + in->sun[2] * in->sun[2];
+    if (!(len2 > 0.0f)) return fail(ctx, VT_ERR_ARG, "sun direction must be nonzero");
+    if (world->dist_dirty) {
+        vt_status s = rebuild_distances(const_cast<vt_world*>(world), st);
+        if (s) return s;
+    }
+    vt_params p;
+    vt_params_default(&p);
+    for (int j = 0; j < 3; ++j) p.sun_dir[j] = in->sun[j];
+    a.w = world->view();
+    a.f = make_frame(cam, &p);
+    a.hits = reinterpret_cast<const uint4*>(d_hits);
+    a.pal = in->d_palette;
+    a.alb = in->d_albedo;
+    for (int j = 0; j < 3; ++j) {
+        a.sun[j] = in->sun[j];
+        a.sun_n[j] = a.f.sun_n[j];
+    }
+    a.inv_len = 1.0f / sqrtf(len2);
+    a.ka = in->ambient;
+    a.kd = in->diffuse;
+    a.shadow_steps = in->shadow_max_steps;
+    const dim3 grid((cam->width + 15) / 16, (cam->height + 15) / 16);
+    const size_t dist_bytes = (size_t)((a.w.nchunks + 15u) / 16u) * 16u;
+    const bool smem_dist = dist_bytes <= kMaxSharedDist;
+    const size_t smem = 776 * sizeof(float) + (smem_dist ? dist_bytes : 0);
+    if (bwd) {
+        if (smem_dist) k_shade<true, true><<<grid, kAdjBlock, smem, st>>>(a);
+        else k_shade<true, false><<<grid, kAdjBlock, smem, st>>>(a);
+    } else {
+        if (smem_dist) k_shade<false, true><<<grid, kAdjBlock, smem, st>>>(a);
+        else k_shade<false, false><<<grid, kAdjBlock, smem, st>>>(a);
+    }
+    VT_CUDA(ctx, cudaGetLastError());
+    return VT_OK;
+}
+
+}  // namespace
+
+}  // namespace vt
+
+using namespace vt;
+
+extern "C" {
+
+vt_status vt_shade_forward(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_hit* d_hits,
+                           const vt_shade_inputs* in, const uint8_t* d_vis_in, uint8_t* d_vis_out, float* d_rgb,
+                           vt_stream stream) {
+    if (!ctx) return VT_ERR_ARG;
+    if (!d_rgb) return fail(ctx, VT_ERR_ARG, "null output image");
+    AdjArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.vis_in = d_vis_in;
+    a.vis_out = d_vis_out;
+    a.rgb = d_rgb;
+    return launch_shade(ctx, world, cam, d_hits, in, a, false, (cudaStream_t)stream);
+}
+
+vt_status vt_shade_backward(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_hit* d_hits,
+                            const vt_shade_inputs* in, const float* d_target, float* d_loss, float* d_grad_palette,
+                            float* d_grad_albedo, float* d_grad_sun, vt_stream stream) {
+    if (!ctx) return VT_ERR_ARG;
+    if (!d_target || !d_loss || !d_grad_palette || !d_grad_sun)
+        return fail(ctx, VT_ERR_ARG, "null target, loss or gradient buffer");
+    AdjArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.target = d_target;
+    a.loss = d_loss;
+    a.gpal = d_grad_palette;
+    a.galb = d_grad_albedo;
+    a.gsun = d_grad_sun;
+    return launch_shade(ctx, world, cam, d_hits, in, a, true, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -215,6 +215,9 @@ __device__ __forceinline__ unsigned composite(const FrameParams& f, int px, int 
     return unorm8(col[0]) | (unorm8(col[1]) << 8) | (unorm8(col[2]) << 16) | (unorm8(col[3]) << 24);
 }
 
+// FrameParams of a camera and parameter set (render.cu).
+FrameParams make_frame(const vt_camera* cam, const vt_params* p);
+
 // The per-frame constants of FrameParams (host side).
 inline void frame_constants(FrameParams& f) {
     normalize3(f.sun, f.sun_n);

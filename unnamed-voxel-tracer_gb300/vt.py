@@ -65,6 +65,11 @@ class Tuning_t(C.Structure):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
 
 
+class ShadeInputs_t(C.Structure):
+    _fields_ = [("d_palette", C.c_void_p), ("d_albedo", C.c_void_p), ("sun", C.c_float * 3),
+                ("ambient", C.c_float), ("diffuse", C.c_float), ("shadow_max_steps", C.c_int32)]
+
+
 class WorldDesc_t(C.Structure):
     _fields_ = [("dims", C.c_int32 * 3)]
 
@@ -123,6 +128,8 @@ _SIGNATURES = {
     "vt_render_host_static": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), _P]),
     "vt_render_stats": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), C.POINTER(Stats_t), _P]),
     "vt_trace_rays": (_S, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, _P]),
+    "vt_shade_forward": (_S, [_P, _P, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P, _P, _P]),
+    "vt_shade_backward": (_S, [_P, _P, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P, _P, _P, _P, _P]),
     "vt_set_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
     "vt_get_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
     "vt_autotune": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), C.c_int32, C.c_char_p,
@@ -368,6 +375,72 @@ def render_host(ctx: Context, world: World, cam: Camera_t, params: Params_t, out
     assert out.dtype == HIT_DTYPE and out.size >= cam.width * cam.height
     ctx.check(ctx.lib.vt_render_host(ctx.handle, world.handle, C.byref(cam), C.byref(params), _ptr(out)))
     return out
+
+
+class Shading:
+    """Differentiable Lambert shading of one world (vt_shade_forward/backward),
+    the C-ABI counterpart of a torch.autograd.Function: forward() renders the
+    image from the fixed primary hits, backward() the loss and its gradients.
+    Parameters live in device buffers owned here; gradients accumulate until
+    zero_grad()."""
+
+    def __init__(self, ctx: Context, world: World, palette: np.ndarray, albedo: np.ndarray | None, sun,
+                 ambient: float = 0.2, diffuse: float = 0.8, shadow_max_steps: int = 512):
+        self.ctx, self.world = ctx, world
+        X, Y, Z = world.dims
+        self.d_pal = ctx.alloc(256 * 3 * 4)
+        self.d_alb = ctx.alloc(X * Y * Z * 4) if albedo is not None else None
+        self.d_gpal = ctx.alloc(256 * 3 * 4)
+        self.d_galb = ctx.alloc(X * Y * Z * 4) if albedo is not None else None
+        self.d_gsun = ctx.alloc(3 * 4)
+        self.d_loss = ctx.alloc(4)
+        self.inputs = ShadeInputs_t()
+        self.set_params(palette, albedo, sun)
+        self.inputs.ambient, self.inputs.diffuse = float(ambient), float(diffuse)
+        self.inputs.shadow_max_steps = int(shadow_max_steps)
+        self.zero_grad()
+
+    def set_params(self, palette, albedo, sun) -> None:
+        self.d_pal.upload(np.asarray(palette, np.float32).reshape(256, 3))
+        if albedo is not None:
+            self.d_alb.upload(np.asarray(albedo, np.float32).reshape(-1))
+        self.inputs.d_palette = self.d_pal.ptr
+        self.inputs.d_albedo = self.d_alb.ptr if self.d_alb is not None else None
+        self.inputs.sun = (C.c_float * 3)(*[float(s) for s in sun])
+
+    def zero_grad(self) -> None:
+        for b in (self.d_gpal, self.d_galb, self.d_gsun, self.d_loss):
+            if b is not None:
+                b.zero()
+        self.ctx.sync()
+
+    def forward(self, cam: Camera_t, d_hits: DeviceBuffer, d_rgb: DeviceBuffer, vis_in=None, vis_out=None,
+                stream=None) -> None:
+        self.ctx.check(self.ctx.lib.vt_shade_forward(
+            self.ctx.handle, self.world.handle, C.byref(cam), d_hits.ptr, C.byref(self.inputs),
+            vis_in.ptr if vis_in is not None else None, vis_out.ptr if vis_out is not None else None, d_rgb.ptr,
+            stream))
+
+    def backward(self, cam: Camera_t, d_hits: DeviceBuffer, d_target: DeviceBuffer, stream=None) -> None:
+        self.ctx.check(self.ctx.lib.vt_shade_backward(
+            self.ctx.handle, self.world.handle, C.byref(cam), d_hits.ptr, C.byref(self.inputs), d_target.ptr,
+            self.d_loss.ptr, self.d_gpal.ptr, self.d_galb.ptr if self.d_galb is not None else None,
+            self.d_gsun.ptr, stream))
+
+    def grads(self) -> dict:
+        self.ctx.sync()
+        out = {"loss": float(self.d_loss.download(np.zeros(1, np.float32))[0]),
+               "palette": self.d_gpal.download(np.zeros((256, 3), np.float32)),
+               "sun": self.d_gsun.download(np.zeros(3, np.float32))}
+        if self.d_galb is not None:
+            out["albedo"] = self.d_galb.download(np.zeros(self.world.dims[0] * self.world.dims[1]
+                                                          * self.world.dims[2], np.float32))
+        return out
+
+    def close(self) -> None:
+        for b in (self.d_pal, self.d_alb, self.d_gpal, self.d_galb, self.d_gsun, self.d_loss):
+            if b is not None:
+                b.free()
 
 
 STATIC_MAX_PIXELS = 262144
