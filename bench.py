@@ -188,6 +188,120 @@ def run_reference(args, rank: int, world: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+def _timed(torch, fn, reps: int) -> float:
+    """Mean ms of fn() over reps runs, CUDA events on the current stream."""
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def measure_config2(vt, scenes, ctx, torch, flush) -> dict:
+    """2048x256x2048 world with caves (1 GiB of materials, 128 MiB of mask
+    words: at the L2 size), 3840x2160 primary + shadow + bounce rays."""
+    desc, cams, params = scenes.config2()
+    w = vt.World(ctx, tuple(desc.dims))
+    w.upload_dense(vt.gen_world(desc))
+    out = ctx.alloc(cams[0].width * cams[0].height * 16)
+    sh = torch.cuda.current_stream().cuda_stream
+    stats = [vt.render_stats(ctx, w, c, params, sh) for c in cams]
+    rays = [s["primary_rays"] + s["shadow_rays"] + s["bounce_rays"] for s in stats]
+    abytes = [8 * s["mask_words"] + 8 * s["coarse_words"] + s["material_bytes"] + s["record_bytes"] for s in stats]
+    ms = []
+    for i, c in enumerate(cams):
+        def frame():
+            ctx.check(ctx.lib.vt_render(ctx.handle, w.handle, C.byref(c), C.byref(params), out.ptr, sh))
+        frame()
+        flush.zero_()
+        ms.append(_timed(torch, frame, 1))
+    w.close()
+    out.free()
+    t = sum(ms) * 1e-3
+    return {"workload": "2048x256x2048 world + caves, 3840x2160, primary + shadow + 1 cosine bounce per hit",
+            "grays_per_s": sum(rays) / t / 1e9, "ms_per_frame": sum(ms) / len(ms),
+            "rays_per_frame": sum(rays) / len(rays), "algorithmic_gbs": sum(abytes) / t / 1e9,
+            "l2": "flushed before each frame"}
+
+
+def measure_config3(vt, scenes, ctx, torch) -> dict:
+    """64 cube scenes (edge log-uniform in [32, 512]) x 1-8 cameras: one
+    persistent CUDA-graph launch vs one vt_render launch per camera."""
+    sc, params = scenes.config3()
+    worlds, jobs = [], []
+    for desc, cams in sc:
+        w = vt.World(ctx, tuple(desc.dims))
+        w.upload_dense(vt.gen_world(desc))
+        worlds.append(w)
+        for c in cams:
+            jobs.append((w, c, ctx.alloc(c.width * c.height * 16)))
+    sh = torch.cuda.current_stream().cuda_stream
+
+    def per_scene():
+        for w, c, buf in jobs:
+            ctx.check(ctx.lib.vt_render(ctx.handle, w.handle, C.byref(c), C.byref(params), buf.ptr, sh))
+
+    batch = vt.Batch(ctx, jobs, params)
+    per_scene()
+    batch.launch(sh)
+    t_scene = _timed(torch, per_scene, 3)
+    t_batch = _timed(torch, lambda: batch.launch(sh), 3)
+    pixels = batch.info()["pixels"]
+    batch.close()
+    for _, _, buf in jobs:
+        buf.free()
+    for w in worlds:
+        w.close()
+    return {"workload": f"{len(sc)} scenes, {len(jobs)} cameras, {pixels / 1e6:.1f} Mpixels, primary + shadow",
+            "batched_gpix_per_s": pixels / (t_batch * 1e-3) / 1e9,
+            "per_scene_gpix_per_s": pixels / (t_scene * 1e-3) / 1e9,
+            "batched_ms": t_batch, "per_scene_ms": t_scene, "speedup": t_scene / t_batch,
+            "launches_per_scene_path": len(jobs)}
+
+
+def measure_config4(vt, scenes, ctx, torch) -> dict:
+    """256^3 world, 16 views at 512x512: one optimisation step = fused
+    forward + backward of the shading (shadow rays recomputed) over all views."""
+    desc, cams, (pal, alb, sun), (hpal, hsun) = scenes.config4()
+    w = vt.World(ctx, tuple(desc.dims))
+    w.upload_dense(vt.gen_world(desc))
+    prim = vt.default_params(rays=vt.RAYS_PRIMARY, shade=vt.SHADE_NONE)
+    n = cams[0].width * cams[0].height
+    hits = [ctx.alloc(n * 16) for _ in cams]
+    for c, hb in zip(cams, hits):
+        vt.render(ctx, w, c, prim, hb)
+    targets = [ctx.alloc(n * 12) for _ in cams]
+    hidden = vt.Shading(ctx, w, hpal, alb, hsun)
+    for c, hb, tb in zip(cams, hits, targets):
+        hidden.forward(c, hb, tb)
+    hidden.close()
+    sh_ = vt.Shading(ctx, w, pal, alb, sun)
+    rgb = ctx.alloc(n * 12)
+
+    def step():
+        sh_.zero_grad_async()
+        for c, hb, tb in zip(cams, hits, targets):
+            sh_.backward(c, hb, tb)
+
+    def forward():
+        for c, hb in zip(cams, hits):
+            sh_.forward(c, hb, rgb)
+
+    step()
+    t_step = _timed(torch, step, 5)
+    t_fwd = _timed(torch, forward, 5)
+    loss = sh_.grads()["loss"]
+    sh_.close()
+    for b in hits + targets + [rgb]:
+        b.free()
+    w.close()
+    return {"workload": "256^3 world, 16 views at 512x512, Lambert + shadowed sun, L2 image loss",
+            "fwd_bwd_ms_per_iter": t_step, "fwd_ms_per_iter": t_fwd, "loss": loss}
+
+
 def measure_l2_gbs(torch, dev) -> float:
     """Read+write GB/s of a 24 MiB copy held in L2 (many passes)."""
     a = torch.empty(24 << 20, dtype=torch.uint8, device=dev)
@@ -294,6 +408,19 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         rate, desc, _ = cpu_oracle_sample(vt, oracle_py, mats, cams[0], params, threads, 12.0)
         cpu = {"value": rate / 1e9, "unit": "Grays/s", "cores": threads, "kind": "port", "sample": desc}
     name, sms = ctx.device_info()
+    # the other configurations, measured once each (not part of the timed steps)
+    extra = {}
+    if world == 1 and not args.headline_only:
+        import scenes
+        wobj.close()
+        for key, fn in (("config2", lambda: measure_config2(vt, scenes, ctx, torch, flush)),
+                        ("config3", lambda: measure_config3(vt, scenes, ctx, torch)),
+                        ("config4", lambda: measure_config4(vt, scenes, ctx, torch))):
+            try:
+                extra[key] = fn()
+            except Exception as exc:  # report, keep the headline line
+                extra[key] = {"error": f"{type(exc).__name__}: {exc}"}
+        wobj = None
     line = {
         "metric": "Grays/s", "value": value, "unit": "Grays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -311,9 +438,11 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                 "d2h_bytes_per_step": nbytes,
                 "note": "vt_render_host: camera and params travel in the launch; records copied to pinned host memory"},
         "cpu_baseline": cpu, "clocks": clk.summary(), "device": {"name": name, "sms": sms},
+        **extra,
     }
     print(json.dumps(line), flush=True)
-    wobj.close()
+    if wobj is not None:
+        wobj.close()
     ctx.close()
 
 
@@ -323,6 +452,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the config 2/3/4 measurements that follow the headline")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -235,6 +235,26 @@ typedef struct {
 vt_status vt_render_stats(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
                           const vt_params* params, vt_stats* out, vt_stream stream);
 
+/* ----------------------------------------------------------------- batch
+ * Many scenes x cameras in one launch (no counterpart in the reference, which
+ * renders one camera per frame, game.zig:232-256).  A persistent kernel pulls
+ * 16x16-pixel units of all jobs from one device work queue; every job's
+ * records are identical to what vt_render writes for it alone. */
+typedef struct {
+    const vt_world* world;
+    vt_camera camera;
+    vt_hit* d_out;     /* camera.width * camera.height records */
+} vt_job;
+
+/* Uploads the job table and sizes the launch.  The batch is replayed with
+ * vt_batch_launch, which captures a CUDA graph (queue reset + kernel) on its
+ * first call and launches that graph on the given stream every time. */
+vt_status vt_batch_create(vt_ctx* ctx, const vt_job* jobs, int32_t n, const vt_params* params, vt_batch** out);
+vt_status vt_batch_launch(vt_batch* batch, vt_stream stream);
+vt_status vt_batch_destroy(vt_batch* batch);
+/* Pixels (= primary rays), jobs and 16x16 work units of one launch. */
+vt_status vt_batch_info(const vt_batch* batch, uint64_t* pixels, int32_t* jobs, uint32_t* units);
+
 /* ------------------------------------------------------- shading adjoint
  * No counterpart in the reference (its shading is fixed-function,
  * blit.fragment.glsl:31).  Lambert + shadowed sun over the primary hits of a

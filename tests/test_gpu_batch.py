@@ -1,0 +1,42 @@
+"""The batched persistent launch (vt_batch_*): many worlds of different sizes,
+several cameras each at different resolutions, one CUDA-graph launch.  Every
+job's records must equal what vt_render writes for that job alone (and hence
+the oracle's, which test_gpu_render checks for vt_render)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_matches_per_job_renders(vt, ctx, oracle):
+    rng = np.random.default_rng(31)
+    worlds, jobs, outs = [], [], []
+    params = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=vt.gen_sun(31))
+    for s in range(6):
+        edge = int(rng.integers(32, 200))
+        d = vt.gen_desc((edge, edge, edge), scale=edge / 128.0, seed=500 + s)
+        w = vt.World(ctx, (edge, edge, edge))
+        w.upload_dense(vt.gen_world(d))
+        worlds.append(w)
+        for c in range(int(rng.integers(1, 4))):
+            W, H = [(96, 64), (160, 120), (200, 75), (33, 17)][int(rng.integers(0, 4))]
+            cam = vt.gen_camera(d, c, W, H)
+            buf = ctx.alloc(W * H * 16)
+            jobs.append((w, cam, buf))
+    batch = vt.Batch(ctx, jobs, params)
+    info = batch.info()
+    assert info["jobs"] == len(jobs)
+    for rep in range(3):   # graph replays reuse the queue counter
+        for _, cam, buf in jobs:
+            buf.zero()
+        batch.launch()
+        ctx.sync()
+        for w, cam, buf in jobs:
+            got = buf.download(np.zeros(cam.width * cam.height, vt.HIT_DTYPE))
+            want = vt.render_host(ctx, w, cam, params)
+            assert np.array_equal(got, want)
+    batch.close()
+    for _, _, buf in jobs:
+        buf.free()
+    for w in worlds:
+        w.close()

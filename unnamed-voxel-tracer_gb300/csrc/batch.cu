@@ -1,0 +1,179 @@
+// batch.cu -- many scenes x cameras in one persistent launch.
+//
+// Every job (a world, a camera, an output buffer) is cut into 16 x 16 pixel
+// units; the units of all jobs are numbered consecutively, job after job.  A
+// persistent grid (SMs x resident blocks) runs until a device counter hands out
+// the last unit: a warp takes one unit at a time, finds its job by binary
+// search over the jobs' first-unit numbers, and traces the unit's 256 pixels as
+// eight 8 x 4 tiles, one pixel per lane, with the same per-pixel code as the
+// single-frame kernel (render_pixel.cuh).  Large and small frames of worlds of
+// very different sizes therefore share the GPU without per-launch tails, and
+// the whole batch is one CUDA graph launch (counter reset + kernel).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "render_pixel.cuh"
+
+namespace vt {
+
+struct JobDesc {
+    WorldView w;
+    FrameParams f;
+    uint4* out;
+    unsigned first_unit;
+    unsigned units_x;
+};
+
+constexpr int kBatchBlock = 256;
+constexpr int kUnit = 16;  // pixels per unit side
+
+__global__ void __launch_bounds__(kBatchBlock, 4) k_render_batch(const JobDesc* __restrict__ jobs, int njobs,
+                                                                 unsigned total_units, unsigned* __restrict__ counter) {
+    const unsigned lane = threadIdx.x & 31u;
+    for (;;) {
+        unsigned unit = 0;
+        if (lane == 0) unit = atomicAdd(counter, 1u);
+        unit = __shfl_sync(0xFFFFFFFFu, unit, 0);
+        if (unit >= total_units) break;
+        int lo = 0, hi = njobs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&jobs[mid].first_unit) <= unit) lo = mid;
+            else hi = mid - 1;
+        }
+        const JobDesc& J = jobs[lo];
+        const unsigned local = unit - J.first_unit;
+        const int ux = (int)(local % J.units_x) * kUnit, uy = (int)(local / J.units_x) * kUnit;
+        const WorldView w = J.w;
+        const FrameParams f = J.f;
+        for (int sub = 0; sub < 8; ++sub) {
+            const int px = ux + (sub & 1) * 8 + (int)(lane & 7u);
+            const int py = uy + (sub >> 1) * 4 + (int)(lane >> 3);
+            if (px < f.width && py < f.height) {
+                PixelCounters pc;
+                J.out[(size_t)py * f.width + px] =
+                    render_pixel<false, false>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, nullptr, pc);
+            }
+        }
+    }
+}
+
+}  // namespace vt
+
+struct vt_batch {
+    vt_ctx* ctx = nullptr;
+    std::vector<const vt_world*> worlds;
+    vt::JobDesc* d_jobs = nullptr;
+    unsigned* d_counter = nullptr;
+    int njobs = 0;
+    unsigned total_units = 0;
+    unsigned long long pixels = 0;
+    unsigned blocks = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+using namespace vt;
+
+extern "C" {
+
+vt_status vt_batch_create(vt_ctx* ctx, const vt_job* jobs, int32_t n, const vt_params* params, vt_batch** out) {
+    if (!ctx) return VT_ERR_ARG;
+    if (!jobs || !params || !out || n <= 0) return fail(ctx, VT_ERR_ARG, "bad batch arguments");
+    *out = nullptr;
+    std::vector<JobDesc> host((size_t)n);
+    unsigned long long units = 0, pixels = 0;
+    vt_batch* b = new (std::nothrow) vt_batch();
+    if (!b) return fail(ctx, VT_ERR_OOM, "host allocation failed");
+    for (int i = 0; i < n; ++i) {
+        const vt_job& j = jobs[i];
+        vt_status s = check_frame_args(ctx, j.world, &j.camera, params);
+        if (!s && !j.d_out) s = fail(ctx, VT_ERR_ARG, "null job output");
+        if (s) {
+            delete b;
+            return s;
+        }
+        JobDesc& d = host[(size_t)i];
+        d.w = j.world->view();
+        d.f = make_frame(&j.camera, params);
+        d.out = reinterpret_cast<uint4*>(j.d_out);
+        d.first_unit = (unsigned)units;
+        d.units_x = (unsigned)((j.camera.width + kUnit - 1) / kUnit);
+        units += (unsigned long long)d.units_x * (unsigned)((j.camera.height + kUnit - 1) / kUnit);
+        pixels += (unsigned long long)j.camera.width * (unsigned long long)j.camera.height;
+        b->worlds.push_back(j.world);
+    }
+    if (units >= (1ull << 32)) {
+        delete b;
+        return fail(ctx, VT_ERR_ARG, "batch too large (units >= 2^32)");
+    }
+    cudaError_t e;
+    if ((e = cudaMalloc(&b->d_jobs, host.size() * sizeof(JobDesc))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_counter, sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMemcpy(b->d_jobs, host.data(), host.size() * sizeof(JobDesc), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        vt_batch_destroy(b);
+        return check_cuda(ctx, e, "batch upload");
+    }
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_batch, kBatchBlock, 0)) != cudaSuccess) {
+        vt_batch_destroy(b);
+        return check_cuda(ctx, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    }
+    b->ctx = ctx;
+    b->njobs = n;
+    b->total_units = (unsigned)units;
+    b->pixels = pixels;
+    b->blocks = (unsigned)(ctx->sm_count * std::max(per_sm, 1));
+    *out = b;
+    return VT_OK;
+}
+
+vt_status vt_batch_launch(vt_batch* b, vt_stream stream) {
+    if (!b) return VT_ERR_ARG;
+    vt_ctx* ctx = b->ctx;
+    cudaStream_t st = (cudaStream_t)stream;
+    // stale empty-space distances are rebuilt before (outside) the graph
+    for (const vt_world* w : b->worlds)
+        if (w->dist_dirty) {
+            vt_status s = rebuild_distances(const_cast<vt_world*>(w), st);
+            if (s) return s;
+        }
+    if (!b->exec) {
+        // capture on a private stream: the legacy default stream cannot be captured
+        cudaStream_t cap = nullptr;
+        VT_CUDA(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), cap);
+            k_render_batch<<<b->blocks, kBatchBlock, 0, cap>>>(b->d_jobs, b->njobs, b->total_units, b->d_counter);
+            e = cudaStreamEndCapture(cap, &b->graph);
+        }
+        cudaStreamDestroy(cap);
+        if (e != cudaSuccess) return check_cuda(ctx, e, "batch graph capture");
+        VT_CUDA(ctx, cudaGraphInstantiate(&b->exec, b->graph, 0));
+    }
+    VT_CUDA(ctx, cudaGraphLaunch(b->exec, st));
+    return VT_OK;
+}
+
+vt_status vt_batch_destroy(vt_batch* b) {
+    if (!b) return VT_ERR_ARG;
+    cudaDeviceSynchronize();
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->d_jobs) cudaFree(b->d_jobs);
+    if (b->d_counter) cudaFree(b->d_counter);
+    delete b;
+    return VT_OK;
+}
+
+vt_status vt_batch_info(const vt_batch* b, uint64_t* pixels, int32_t* jobs, uint32_t* units) {
+    if (!b) return VT_ERR_ARG;
+    if (pixels) *pixels = b->pixels;
+    if (jobs) *jobs = b->njobs;
+    if (units) *units = b->total_units;
+    return VT_OK;
+}
+
+}  // extern "C"

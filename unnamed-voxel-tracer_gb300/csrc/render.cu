@@ -10,8 +10,7 @@
 // record; nothing goes through memory between the passes.
 #include <cstring>
 
-#include "shade.cuh"
-#include "trace_p.cuh"
+#include "render_pixel.cuh"
 
 namespace vt {
 
@@ -19,102 +18,6 @@ namespace vt {
 // start close together and share brick words in L1.
 constexpr int kBlock = 256;
 constexpr size_t kMaxSharedCoarse = 48 * 1024;
-
-struct PixelCounters {
-    unsigned v[kNumCounters];
-};
-
-// The instrumented and bounds-checked variants run the three-level model
-// traversal (it defines the algorithmic byte counts); the production variant
-// runs trace_fast.  Both give identical results.
-template <bool STATS, bool CHECKED, bool MAT, class Coarse>
-__device__ __forceinline__ bool trace_any(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
-                                          const PRay& r, int max_steps, TraceHit& h, TraceCounters& cnt,
-                                          unsigned* status) {
-    if (STATS || CHECKED) return trace_p<STATS, CHECKED, MAT>(w, coarse, r, max_steps, h, cnt, status);
-    return trace_fast<MAT>(w, cd, r, max_steps, h);
-}
-
-template <bool STATS, bool CHECKED, class Coarse>
-__device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
-                                              const FrameParams& f, int px, int py, unsigned* status,
-                                              PixelCounters& pc) {
-    float o[3], d[3];
-    primary_ray(f, px, py, o, d);
-    PRay r;
-    pray_init(r, o, d);
-    TraceHit h;
-    TraceCounters cnt;
-    const bool hit = trace_any<STATS, CHECKED, true>(w, coarse, cd, r, f.max_steps, h, cnt, status);
-    if (STATS) {
-        pc.v[0] += 1;
-        pc.v[9] += 16;
-    }
-    unsigned flags = 0, rgba, voxel = 0xFFFFFFFFu, face = 0xFFu, mat = 0;
-    float t = -1.0f;
-    float col[4];
-    if (hit) {
-        flags = VT_HIT_PRIMARY;
-        voxel = (unsigned)h.c[0] + (unsigned)w.dims[0] * ((unsigned)h.c[1] + (unsigned)w.dims[1] * (unsigned)h.c[2]);
-        t = h.t;
-        const int e = h.axis;
-        const bool pe = e == 0 ? r.pos[0] : (e == 1 ? r.pos[1] : r.pos[2]);
-        face = 2u * (unsigned)e + (pe ? 0u : 1u);
-        mat = h.mat;
-        const unsigned alb = __ldg(w.palette + mat);
-        if (STATS) {
-            pc.v[1] += 1;
-            pc.v[8] += 1;
-        }
-        float nrm[3], so[3];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            nrm[j] = (j == e) ? (pe ? -1.0f : 1.0f) : 0.0f;
-            so[j] = __fmaf_rn(r.d[j], t, o[j]);
-            if (j == e) so[j] = so[j] + nrm[j] * 0.001f;
-        }
-        bool shadowed = false;
-        if (f.rays & VT_RAYS_SHADOW) {
-            PRay rs;
-            pray_init(rs, so, f.sun);
-            TraceHit hs;
-            shadowed = trace_any<STATS, CHECKED, false>(w, coarse, cd, rs, f.shadow_max_steps, hs, cnt, status);
-            if (shadowed) flags |= VT_HIT_SHADOWED;
-            if (STATS) {
-                pc.v[2] += 1;
-                pc.v[3] += shadowed ? 1u : 0u;
-            }
-        }
-        bool bounce_open = false;
-        float bdir[3] = {0.0f, 0.0f, 0.0f};
-        if (f.rays & VT_RAYS_BOUNCE) {
-            unsigned seed = ((unsigned)px * 1973u + (unsigned)py * 9277u) ^ f.seed;
-            cosine_hemisphere(nrm, seed, bdir);
-            PRay rb;
-            pray_init(rb, so, bdir);
-            TraceHit hb;
-            const bool bh = trace_any<STATS, CHECKED, false>(w, coarse, cd, rb, f.bounce_max_steps, hb, cnt, status);
-            if (bh) flags |= VT_HIT_BOUNCE;
-            bounce_open = !bh;
-            if (STATS) {
-                pc.v[4] += 1;
-                pc.v[5] += bh ? 1u : 0u;
-            }
-        }
-        shade_hit(f, alb, e, pe, shadowed, bounce_open, bdir, col);
-        rgba = f.shade == VT_SHADE_NONE ? alb : composite(f, px, py, col);
-    } else {
-        shade_miss(f, d, col);
-        rgba = f.shade == VT_SHADE_NONE ? 0u : composite(f, px, py, col);
-    }
-    if (STATS) {
-        pc.v[6] += cnt.mask;
-        pc.v[7] += cnt.coarse;
-        pc.v[10] += cnt.steps;
-        pc.v[11] += cnt.iters;
-    }
-    return make_uint4(voxel, __float_as_uint(t), rgba, face | (mat << 8) | (flags << 16));
-}
 
 template <bool STATS>
 __device__ __forceinline__ void flush_counters(PixelCounters& pc, unsigned long long* counters) {

@@ -70,6 +70,10 @@ class ShadeInputs_t(C.Structure):
                 ("ambient", C.c_float), ("diffuse", C.c_float), ("shadow_max_steps", C.c_int32)]
 
 
+class Job_t(C.Structure):
+    _fields_ = [("world", C.c_void_p), ("camera", Camera_t), ("d_out", C.c_void_p)]
+
+
 class WorldDesc_t(C.Structure):
     _fields_ = [("dims", C.c_int32 * 3)]
 
@@ -130,6 +134,10 @@ _SIGNATURES = {
     "vt_trace_rays": (_S, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, _P]),
     "vt_shade_forward": (_S, [_P, _P, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P, _P, _P]),
     "vt_shade_backward": (_S, [_P, _P, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P, _P, _P, _P, _P]),
+    "vt_batch_create": (_S, [_P, C.POINTER(Job_t), C.c_int32, C.POINTER(Params_t), C.POINTER(_P)]),
+    "vt_batch_launch": (_S, [_P, _P]),
+    "vt_batch_destroy": (_S, [_P]),
+    "vt_batch_info": (_S, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_int32), C.POINTER(C.c_uint32)]),
     "vt_set_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
     "vt_get_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
     "vt_autotune": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), C.c_int32, C.c_char_p,
@@ -377,6 +385,35 @@ def render_host(ctx: Context, world: World, cam: Camera_t, params: Params_t, out
     return out
 
 
+class Batch:
+    """Many (world, camera, output) jobs rendered by one persistent launch,
+    replayed as a CUDA graph (vt_batch_*)."""
+
+    def __init__(self, ctx: Context, jobs, params: Params_t):
+        self.ctx = ctx
+        arr = (Job_t * len(jobs))()
+        for i, (world, cam, d_out) in enumerate(jobs):
+            arr[i].world = world.handle.value if hasattr(world.handle, "value") else world.handle
+            arr[i].camera = cam
+            arr[i].d_out = d_out.ptr
+        h = C.c_void_p()
+        ctx.check(ctx.lib.vt_batch_create(ctx.handle, arr, len(jobs), C.byref(params), C.byref(h)))
+        self.handle = h
+
+    def launch(self, stream=None) -> None:
+        self.ctx.check(self.ctx.lib.vt_batch_launch(self.handle, stream))
+
+    def info(self) -> dict:
+        px, nj, nu = C.c_uint64(), C.c_int32(), C.c_uint32()
+        self.ctx.check(self.ctx.lib.vt_batch_info(self.handle, C.byref(px), C.byref(nj), C.byref(nu)))
+        return {"pixels": px.value, "jobs": nj.value, "units": nu.value}
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.vt_batch_destroy(self.handle)
+            self.handle = None
+
+
 class Shading:
     """Differentiable Lambert shading of one world (vt_shade_forward/backward),
     the C-ABI counterpart of a torch.autograd.Function: forward() renders the
@@ -409,10 +446,13 @@ class Shading:
         self.inputs.sun = (C.c_float * 3)(*[float(s) for s in sun])
 
     def zero_grad(self) -> None:
+        self.zero_grad_async()
+        self.ctx.sync()
+
+    def zero_grad_async(self, stream=None) -> None:
         for b in (self.d_gpal, self.d_galb, self.d_gsun, self.d_loss):
             if b is not None:
-                b.zero()
-        self.ctx.sync()
+                b.zero(stream)
 
     def forward(self, cam: Camera_t, d_hits: DeviceBuffer, d_rgb: DeviceBuffer, vis_in=None, vis_out=None,
                 stream=None) -> None:
