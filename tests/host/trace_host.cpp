@@ -27,9 +27,10 @@ static inline unsigned atomicOr(unsigned* p, unsigned v) { unsigned o = *p; *p |
 
 #include "../../unnamed-voxel-tracer_gb300/csrc/trace_p.cuh"
 
-// Chebyshev distance (capped at kDistCap + 1) from each cell of a gx*gy*gz
-// occupancy grid to the nearest occupied cell, by brute force over the window.
-static std::vector<unsigned char> cheb(const std::vector<unsigned char>& occ, int gx, int gy, int gz) {
+// Distance max(|dx|, wy*|dy|, |dz|) (capped at kDistCap + 1) from each cell of
+// a gx*gy*gz occupancy grid to the nearest occupied cell, by brute force over
+// growing shells.
+static std::vector<unsigned char> cheb(const std::vector<unsigned char>& occ, int gx, int gy, int gz, int wy) {
     const int cap = vt::kDistCap;
     std::vector<unsigned char> d((size_t)gx * gy * gz);
     for (int z = 0; z < gz; ++z)
@@ -40,7 +41,7 @@ static std::vector<unsigned char> cheb(const std::vector<unsigned char>& occ, in
                     for (int dz = -r; dz <= r && best > cap; ++dz)
                         for (int dy = -r; dy <= r && best > cap; ++dy)
                             for (int dx = -r; dx <= r; ++dx) {
-                                if (std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz))) != r) continue;
+                                if (std::max(std::abs(dx), std::max(wy * std::abs(dy), std::abs(dz))) != r) continue;
                                 int qx = x + dx, qy = y + dy, qz = z + dz;
                                 if (qx < 0 || qy < 0 || qz < 0 || qx >= gx || qy >= gy || qz >= gz) continue;
                                 if (occ[(size_t)qx + (size_t)gx * ((size_t)qy + (size_t)gy * qz)]) { best = r; break; }
@@ -91,7 +92,7 @@ extern "C" int ht_trace_rays(const int32_t dims[3], const uint8_t* dense, const 
                 bocc[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] = mask[ci * 512 + bi] != 0;
                 if (mask[ci * 512 + bi]) cocc[ci] = 1;
             }
-    std::vector<unsigned char> bd = cheb(bocc, gx, gy, gz), cdd = cheb(cocc, cd[0], cd[1], cd[2]);
+    std::vector<unsigned char> bd = cheb(bocc, gx, gy, gz, vt::kFlatY), cdd = cheb(cocc, cd[0], cd[1], cd[2], 1);
     std::vector<unsigned char> bdist(nch * 512);
     for (int z = 0; z < gz; ++z)
         for (int y = 0; y < gy; ++y)

@@ -279,6 +279,12 @@ __device__ __forceinline__ bool trace_p(const WorldView& w, const Coarse& coarse
 // The walk is resumable one iteration at a time (step), so that a persistent
 // kernel can interleave rays of different pixels and kinds in one warp.
 // cdist is the per-chunk distance array (in shared memory in the kernels).
+// Host builds of this header (the traversal tests) may count the kinds of
+// steps (0 chunk jump, 1 brick jump, 2 voxel test + unit step).
+#ifndef VT_STEP_HOOK
+#define VT_STEP_HOOK(kind)
+#endif
+
 struct Walker {
     PRay r;
     int max_steps;
@@ -347,6 +353,7 @@ struct Walker {
         }
         if (!jump) {
             // inside an occupied brick: test the voxel, else one unit crossing
+            VT_STEP_HOOK(2);
             const unsigned half = (vb & 32u) ? (unsigned)(word >> 32) : (unsigned)word;
             if ((half >> (vb & 31u)) & 1u) {
 #pragma unroll
@@ -385,12 +392,16 @@ struct Walker {
             return kMore;
         }
         // leave the empty box of radius rad - 1 units of 2^sh around the unit of c
+        VT_STEP_HOOK(sh == 5 ? 0 : 1);
         int K[3];
         float tK[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             const int u = c[i] >> sh;
-            K[i] = r.pos[i] ? (u + rad) * (1 << sh) : (u - (rad - 1)) * (1 << sh);
+            // a brick distance d promises the box of radius d-1 across and
+            // (d-1)/kFlatY vertically (kFlatY-weighted Chebyshev distance)
+            const int ri = (i == 1 && sh == 2) ? (rad - 1) / kFlatY + 1 : rad;
+            K[i] = r.pos[i] ? (u + ri) * (1 << sh) : (u - (ri - 1)) * (1 << sh);
             tK[i] = ptime(r, i, K[i]);
         }
         const int e = tK[0] < tK[1] ? (tK[0] < tK[2] ? 0 : 2) : (tK[1] < tK[2] ? 1 : 2);

@@ -39,8 +39,13 @@ struct WorldView {
 };
 
 // Cap of the empty-space distances: a stored value d >= 1 promises that every
-// brick (chunk) within Chebyshev radius d - 1 is empty.
+// brick (chunk) within radius d - 1 is empty.
 constexpr int kDistCap = 15;
+// The brick distance weighs vertical offsets by kFlatY: d = min over occupied
+// bricks of max(|dx|, kFlatY*|dy|, |dz|).  Its empty box is flat and wide
+// (radius d-1 across, (d-1)/kFlatY up and down), which suits rays that skim
+// terrain; the chunk distance is plain Chebyshev.
+constexpr int kFlatY = 4;
 
 }  // namespace vt
 

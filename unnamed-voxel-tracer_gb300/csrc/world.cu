@@ -123,7 +123,7 @@ __global__ void k_dist_pass(const unsigned long long* __restrict__ mask, const u
             } else {
                 v = in[idx];
             }
-            const int m = max(abs(dd), v);
+            const int m = max((level == 0 && axis == 1 ? kFlatY : 1) * abs(dd), v);
             best = min(best, m);
         }
         p[axis] = u;
