@@ -235,6 +235,58 @@ typedef struct {
 vt_status vt_render_stats(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
                           const vt_params* params, vt_stats* out, vt_stream stream);
 
+/* -------------------------------------------------------------- mode R
+ * The reference's own world format and frame, on the GPU, bit for bit:
+ *   map     64^3 table of brick indices (0 = empty, else brick + 1), index
+ *           x + 64*(y + 64*z) (voxel.zig:21-23); bricks of 8^3 u32 voxels
+ *           {ty:28, is_solid:1} indexed x + 8*y + 64*z (voxel.zig:58-61);
+ *           a 512^3 voxel map (MAP_DIMENSION, map.glsl:2)
+ *   atlas   8^3 RGBA8 models; model ty sits at ((ty&31)*8, (ty>>5&31)*8,
+ *           (ty>>10&31)*8) of a 256^3 image (voxel.zig:94-112, map.glsl:57-60)
+ *   frame   primary.comp.glsl (traceMap, 192 steps) -> G-buffer;
+ *           secondary.comp.glsl (traceMap toward SUN_DIR, 48 steps, plus
+ *           traceEntities) -> illumination; blit.fragment.glsl -> colour. */
+typedef struct {
+    uint32_t albedo;       /* frameColor, RGBA8 */
+    uint32_t normal;       /* frameNormal, RGBA8 (negative components store as 0) */
+    uint32_t illumination; /* frameIllumination, RGBA8 */
+    uint32_t color;        /* blit output, RGBA8 */
+    float    position[4];  /* framePosition, RGBA32F */
+} vt_ref_pixel;            /* 32 bytes */
+
+typedef struct {
+    uint32_t data;         /* HitInfo.data: RGBA8 of the hit sub-voxel, 0 on a miss */
+    float    hit_pos[3];   /* sub-voxel position, -1 on a miss */
+    float    normal[3];
+    int32_t  pad;
+} vt_ref_hit;              /* 32 bytes */
+
+/* VoxelBrickmap(512, 8).init + VoxelModelAtlas.init: an empty map and atlas. */
+vt_status vt_brickmap_create(vt_ctx* ctx, vt_brickmap** out);
+vt_status vt_brickmap_destroy(vt_brickmap* bm);
+/* The whole map: h_chunks (64^3 u32) and h_bricks (nbricks * 512 u32). */
+vt_status vt_brickmap_upload(vt_brickmap* bm, const uint32_t* h_chunks, const uint32_t* h_bricks, size_t nbricks);
+/* One 8^3 model (512 RGBA8 texels, x + 8*(y + 8*z)) into atlas slot `slot`. */
+vt_status vt_brickmap_set_model(vt_brickmap* bm, int32_t slot, const uint32_t* h_texels);
+/* VoxelModelAtlas.load_block_model (voxel.zig:94-127): parses a MagicaVoxel
+ * file from memory and appends its models at the next free slots (the file's
+ * y and z axes swapped, colours from its RGBA chunk).  *models_loaded gets
+ * the count. */
+vt_status vt_brickmap_load_vox(vt_brickmap* bm, const uint8_t* h_bytes, size_t nbytes, int32_t* models_loaded);
+/* The same parse into host memory (no device needed): up to max_models
+ * models of 512 texels each into h_texels; *models gets the file's count. */
+vt_status vt_vox_decode(const uint8_t* h_bytes, size_t nbytes, uint32_t* h_texels, int32_t max_models,
+                        int32_t* models);
+/* traceMap (map.glsl:83-168) over an explicit ray list (origins in world
+ * units, n*3 floats each). */
+vt_status vt_trace_map(vt_ctx* ctx, const vt_brickmap* bm, const float* d_origins, const float* d_dirs, int32_t n,
+                       int32_t max_steps, vt_ref_hit* d_out, vt_stream stream);
+/* One reference frame (game.zig:232-256) for a camera: cam.pos, cam.view (the
+ * uniform's matrix) and cam.fov as the reference's UniformData; width*height
+ * vt_ref_pixel records on the device.  Rows are the GL image's rows. */
+vt_status vt_render_reference(vt_ctx* ctx, const vt_brickmap* bm, const vt_camera* cam, vt_ref_pixel* d_out,
+                              vt_stream stream);
+
 /* ----------------------------------------------------------------- batch
  * Many scenes x cameras in one launch (no counterpart in the reference, which
  * renders one camera per frame, game.zig:232-256).  A persistent kernel pulls

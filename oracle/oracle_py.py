@@ -75,6 +75,11 @@ def load() -> C.CDLL:
                                            C.POINTER(C.c_double), C.c_double, C.c_double, C.c_int32, P, P, P, P,
                                            P, P, P, C.POINTER(C.c_double)]
         lib.vto_shade_grad_f64.restype = C.c_int32
+        lib.vto_trace_entities.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
+                                           C.POINTER(VtoRefHit_t)]
+        lib.vto_sky_ref.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        lib.vto_render_reference.argtypes = [C.POINTER(VtoRefWorld_t), C.POINTER(C.c_float),
+                                             C.POINTER(C.c_float), C.c_float, C.c_int32, C.c_int32, P]
         _lib = lib
     return _lib
 
@@ -170,6 +175,26 @@ def shade_grad_f64(world: OracleWorld, cam, hits: np.ndarray, palette, albedo, s
         raise ValueError("bad shading arguments")
     return {"rgb": rgb.reshape(n, 3), "vis": vis, "loss": float(loss[0]), "palette": g_pal.reshape(256, 3),
             "albedo": g_alb, "sun": np.array(list(g_sun))}
+
+
+def render_reference(world: OracleRefWorld, cam) -> np.ndarray:
+    """The reference's frame (primary + secondary + blit), vt.REF_PIXEL_DTYPE records."""
+    out = np.zeros(cam.width * cam.height, dtype=vt.REF_PIXEL_DTYPE)
+    load().vto_render_reference(C.byref(world.w), (C.c_float * 4)(*cam.pos), (C.c_float * 16)(*cam.view), cam.fov,
+                                cam.width, cam.height, out.ctypes.data)
+    return out
+
+
+def trace_entities(o, d, max_distance: float) -> VtoRefHit_t:
+    h = VtoRefHit_t()
+    load().vto_trace_entities((C.c_float * 3)(*o), (C.c_float * 3)(*d), max_distance, C.byref(h))
+    return h
+
+
+def sky_ref(rd):
+    out = (C.c_float * 4)()
+    load().vto_sky_ref((C.c_float * 3)(*rd), out)
+    return list(out)
 
 
 def primary_r(world: OracleRefWorld, cam_pos, view, fov: float, px: int, py: int, width: int, height: int,

@@ -409,7 +409,8 @@ static void shade_pixel(const vto_world* w, const uint32_t* palette, const vt_ca
             }
         }
         if (p->shade == VT_SHADE_REFERENCE) {
-            /* illumination.a stored in RGBA8: +0.3 -> 77/255, -0.3 -> 0
+            /* illumination.a stored in RGBA8: +0.3 -> 76/255 (0.3f * 255
+             * rounds to 76.5, ties to even), -0.3 -> 0
              * (secondary.comp.glsl:45-48, gbuffer.zig:13) */
             float a = shadowed ? 0.0f : (float)unorm8(0.3f) / 255.0f;
             float sq[3];
@@ -751,4 +752,135 @@ void vto_primary_r(const vto_refworld* w, const float cam_pos[4], const float vi
     for (int i = 0; i < 3; ++i) start[i] = (o[i] + d[i] * s) - 0.001f;
     for (int i = 0; i < 3; ++i) dir_out[i] = d[i];
     vto_tracemap(w, start, d, max_steps, out);
+}
+
+/* ---------------------------------------------------------------------
+ * The reference frame restated: secondary.comp.glsl, traceEntities,
+ * SkyDome2 with powf, blit.fragment.glsl.  Images are RGBA8 except the
+ * position (RGBA32F); stores round to nearest (rintf) after clamping.
+ * --------------------------------------------------------------------- */
+static const float kSunDir[3] = {7.52185881e-01f, 6.58950984e-01f, 7.52185881e-01f}; /* camera.glsl:8 */
+
+static void aabb(const float o[3], const float d[3], const float lo[3], const float hi[3], float* tnear, float* tfar) {
+    float t1[3], t2[3];
+    for (int i = 0; i < 3; ++i) {
+        const float a = (lo[i] - o[i]) / d[i];
+        const float b = (hi[i] - o[i]) / d[i];
+        t1[i] = fmin_g(a, b);
+        t2[i] = fmax_g(a, b);
+    }
+    *tnear = fmax_g(fmax_g(t1[0], t1[1]), t1[2]);
+    *tfar = fmin_g(fmin_g(t2[0], t2[1]), t2[2]);
+}
+
+static float dist3(const float a[3], const float b[3]) {
+    const float x = a[0] - b[0], y = a[1] - b[1], z = a[2] - b[2];
+    return sqrtf((x * x + y * y) + z * z);
+}
+
+void vto_trace_entities(const float o[3], const float d[3], float max_distance, vto_refhit* out) {
+    static const float pos[5][3] = {{256.f, 21.f, 256.f}, {251.f, 21.f, 259.f}, {253.f, 21.f, 256.f},
+                                    {251.f, 21.f, 256.f}, {257.f, 21.f, 261.f}};
+    float prev = 1.0f / 0.0f;
+    uint32_t id = 0xFFFFFFFFu;
+    for (int i = 0; i < 5; ++i) {
+        if (dist3(o, pos[i]) >= max_distance) continue;
+        const float hi[3] = {pos[i][0] + 1.0f, pos[i][1] + 1.0f, pos[i][2] + 1.0f};
+        float tn, tf;
+        aabb(o, d, pos[i], hi, &tn, &tf);
+        if (tf >= tn && prev >= tf) {
+            id = (uint32_t)i;
+            prev = tf;
+        }
+    }
+    memset(out, 0, sizeof(*out));
+    if (id != 0xFFFFFFFFu) {
+        const float hi[3] = {pos[id][0] + 1.0f, pos[id][1] + 1.0f, pos[id][2] + 1.0f};
+        float tn, tf;
+        aabb(o, d, pos[id], hi, &tn, &tf);
+        if (tf >= tn) {
+            out->data = 0xFFFFFFFFu;
+            for (int k = 0; k < 3; ++k) out->hit_pos[k] = pos[id][k];
+        }
+    }
+}
+
+void vto_sky_ref(const float rd[3], float out[4]) {
+    float sn[3], rn[3];
+    normalize3(kSunDir, sn);
+    normalize3(rd, rn);
+    const float s = clampf(dot3(sn, rn), 0.0f, 1.2f);
+    const float dy = rd[1] * 0.2f;
+    const float p8 = powf(s, 8.0f), p3 = powf(s, 3.0f);
+    out[0] = ((0.6f - dy * 1.0f) + (0.15f * 0.5f)) + (0.4f * 1.0f) * p8 + 0.2f * p3;
+    out[1] = ((0.71f - dy * 0.5f) + (0.15f * 0.5f)) + (0.4f * 0.6f) * p8 + 0.08f * p3;
+    out[2] = ((0.75f - dy * 1.0f) + (0.15f * 0.5f)) + (0.4f * 0.1f) * p8 + 0.04f * p3;
+    out[3] = 1.0f;
+}
+
+static uint32_t pack8(const float c[4]) {
+    return unorm8(c[0]) | (unorm8(c[1]) << 8) | (unorm8(c[2]) << 16) | (unorm8(c[3]) << 24);
+}
+
+static void unpack8(uint32_t p, float c[4]) {
+    for (int j = 0; j < 4; ++j) c[j] = (float)((p >> (8 * j)) & 255u) / 255.0f;
+}
+
+void vto_render_reference(const vto_refworld* w, const float cam_pos[4], const float view[16], float fov,
+                          int32_t width, int32_t height, vt_ref_pixel* out) {
+    for (int py = 0; py < height; ++py)
+        for (int px = 0; px < width; ++px) {
+            vt_ref_pixel* o = out + (size_t)py * width + px;
+            memset(o, 0, sizeof(*o));
+            /* primary.comp.glsl */
+            float dir[3];
+            vto_refhit h;
+            vto_primary_r(w, cam_pos, view, fov, px, py, width, height, 192, dir, &h);
+            if (h.data != 0) {
+                o->albedo = h.data; /* unpackUnorm4x8 stored back into RGBA8 */
+                const float n4[4] = {h.normal[0], h.normal[1], h.normal[2], 1.0f};
+                o->normal = pack8(n4);
+                for (int k = 0; k < 3; ++k) o->position[k] = ceilf(h.hit_pos[k]) / 8.0f;
+                o->position[3] = 1.0f;
+            } else {
+                float sky4[4];
+                vto_sky_ref(dir, sky4);
+                o->albedo = pack8(sky4);
+                o->normal = 0xFFFFFFFFu;
+                for (int k = 0; k < 4; ++k) o->position[k] = -1.0f;
+            }
+            /* secondary.comp.glsl */
+            if (o->position[0] < 0.0f || o->position[1] < 0.0f || o->position[2] < 0.0f) {
+                o->illumination = 0;
+            } else {
+                float nq[4];
+                unpack8(o->normal, nq);
+                float ro[3];
+                for (int k = 0; k < 3; ++k) ro[k] = o->position[k] + nq[k] * 0.001f;
+                vto_refhit sh, en;
+                vto_tracemap(w, ro, kSunDir, 48, &sh);
+                const float hp8[3] = {sh.hit_pos[0] / 8.0f, sh.hit_pos[1] / 8.0f, sh.hit_pos[2] / 8.0f};
+                vto_trace_entities(ro, kSunDir, dist3(ro, hp8), &en);
+                const float a = (en.data != 0 || sh.data != 0) ? -0.3f : 0.3f;
+                const float il[4] = {kSunDir[0], kSunDir[1], kSunDir[2], a};
+                o->illumination = pack8(il);
+            }
+            /* blit.fragment.glsl */
+            const float u = ((float)px + 0.5f) / (float)width, v = ((float)py + 0.5f) / (float)height;
+            float col[4], nq[4], il[4];
+            unpack8(o->albedo, col);
+            unpack8(o->normal, nq);
+            unpack8(o->illumination, il);
+            float sky4[4];
+            vto_sky_ref(il, sky4); /* SkyDome2(rayPos + normal * 0.001, illumination.xyz): ro is unused */
+            for (int k = 0; k < 4; ++k) col[k] = col[k] + il[3] * sky4[k];
+            const float cu = u - 0.5f, cv = v - 0.5f;
+            if (sqrtf(cu * cu + cv * cv) <= 0.002f) {
+                const float mixc[4] = {1.0f, 1.0f, 1.0f, 0.4f};
+                for (int k = 0; k < 4; ++k) col[k] = col[k] * (1.0f - 0.5f) + mixc[k] * 0.5f;
+            }
+            const float g = powf((u * (1.0f - u)) * (v * (1.0f - v)) * 15.0f, 0.6f * 0.3f);
+            for (int k = 0; k < 4; ++k) col[k] = g * col[k];
+            o->color = pack8(col);
+        }
 }

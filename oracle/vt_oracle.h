@@ -115,6 +115,16 @@ void vto_tracemap(const vto_refworld* w, const float o[3], const float d[3], int
 void vto_primary_r(const vto_refworld* w, const float cam_pos[4], const float view[16], float fov, int32_t px,
                    int32_t py, int32_t width, int32_t height, int32_t max_steps, float dir_out[3], vto_refhit* out);
 
+/* traceEntities (map.glsl:172-201, the part that runs: five unit boxes, the
+ * sentinel 0xFFFFFFFF on a hit). */
+void vto_trace_entities(const float o[3], const float d[3], float max_distance, vto_refhit* out);
+/* SkyDome2 (camera.glsl:11-19) with pow as powf. */
+void vto_sky_ref(const float rd[3], float out[4]);
+/* One reference frame: primary.comp + secondary.comp + blit.fragment for
+ * every pixel of a W x H image (records as vt_ref_pixel). */
+void vto_render_reference(const vto_refworld* w, const float cam_pos[4], const float view[16], float fov,
+                          int32_t width, int32_t height, vt_ref_pixel* out);
+
 #ifdef __cplusplus
 }
 #endif

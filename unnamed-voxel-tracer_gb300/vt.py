@@ -134,6 +134,14 @@ _SIGNATURES = {
     "vt_trace_rays": (_S, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, _P]),
     "vt_shade_forward": (_S, [_P, _P, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P, _P, _P]),
     "vt_shade_backward": (_S, [_P, _P, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P, _P, _P, _P, _P]),
+    "vt_brickmap_create": (_S, [_P, C.POINTER(_P)]),
+    "vt_brickmap_destroy": (_S, [_P]),
+    "vt_brickmap_upload": (_S, [_P, _P, _P, C.c_size_t]),
+    "vt_brickmap_set_model": (_S, [_P, C.c_int32, _P]),
+    "vt_brickmap_load_vox": (_S, [_P, _P, C.c_size_t, C.POINTER(C.c_int32)]),
+    "vt_vox_decode": (_S, [_P, C.c_size_t, _P, C.c_int32, C.POINTER(C.c_int32)]),
+    "vt_trace_map": (_S, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, _P]),
+    "vt_render_reference": (_S, [_P, _P, C.POINTER(Camera_t), _P, _P]),
     "vt_batch_create": (_S, [_P, C.POINTER(Job_t), C.c_int32, C.POINTER(Params_t), C.POINTER(_P)]),
     "vt_batch_launch": (_S, [_P, _P]),
     "vt_batch_destroy": (_S, [_P]),
@@ -383,6 +391,89 @@ def render_host(ctx: Context, world: World, cam: Camera_t, params: Params_t, out
     assert out.dtype == HIT_DTYPE and out.size >= cam.width * cam.height
     ctx.check(ctx.lib.vt_render_host(ctx.handle, world.handle, C.byref(cam), C.byref(params), _ptr(out)))
     return out
+
+
+REF_PIXEL_DTYPE = np.dtype([("albedo", "<u4"), ("normal", "<u4"), ("illumination", "<u4"), ("color", "<u4"),
+                            ("position", "<f4", (4,))])
+REF_HIT_DTYPE = np.dtype([("data", "<u4"), ("hit_pos", "<f4", (3,)), ("normal", "<f4", (3,)), ("pad", "<i4")])
+assert REF_PIXEL_DTYPE.itemsize == 32 and REF_HIT_DTYPE.itemsize == 32
+
+
+def vox_decode(data: bytes) -> np.ndarray:
+    """MagicaVoxel bytes -> (models, 8, 8, 8) [z, y, x] RGBA8 texels, as the
+    reference's model atlas stores them (file y and z swapped)."""
+    buf = np.frombuffer(data, dtype=np.uint8)
+    count = C.c_int32()
+    _check(load().vt_vox_decode(buf.ctypes.data, buf.size, None, 0, C.byref(count)))
+    out = np.zeros((count.value, 8, 8, 8), dtype=np.uint32)
+    _check(load().vt_vox_decode(buf.ctypes.data, buf.size, out.ctypes.data, count.value, C.byref(count)))
+    return out
+
+
+class Brickmap:
+    """The reference's world (VoxelBrickmap(512, 8) + VoxelModelAtlas) on the
+    device, traced with the reference's own traceMap ("mode R")."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        h = C.c_void_p()
+        ctx.check(ctx.lib.vt_brickmap_create(ctx.handle, C.byref(h)))
+        self.handle = h
+
+    def upload(self, chunks: np.ndarray, bricks: np.ndarray) -> None:
+        chunks = np.ascontiguousarray(chunks, np.uint32).reshape(-1)
+        bricks = np.ascontiguousarray(bricks, np.uint32).reshape(-1)
+        assert chunks.size == 64 ** 3 and bricks.size % 512 == 0
+        self.ctx.check(self.ctx.lib.vt_brickmap_upload(self.handle, chunks.ctypes.data, bricks.ctypes.data,
+                                                       bricks.size // 512))
+
+    def set_model(self, slot: int, texels: np.ndarray) -> None:
+        texels = np.ascontiguousarray(texels, np.uint32).reshape(512)
+        self.ctx.check(self.ctx.lib.vt_brickmap_set_model(self.handle, slot, texels.ctypes.data))
+
+    def set_atlas(self, atlas: np.ndarray, slots: int) -> None:
+        """Uploads the first `slots` models of a 256^3 atlas ([z, y, x] or flat)."""
+        a = np.asarray(atlas, np.uint32).reshape(256, 256, 256)
+        for s in range(slots):
+            ox, oy, oz = (s & 31) * 8, ((s >> 5) & 31) * 8, ((s >> 10) & 31) * 8
+            self.set_model(s, a[oz:oz + 8, oy:oy + 8, ox:ox + 8])
+
+    def load_vox(self, data: bytes) -> int:
+        buf = np.frombuffer(data, dtype=np.uint8)
+        n = C.c_int32()
+        self.ctx.check(self.ctx.lib.vt_brickmap_load_vox(self.handle, buf.ctypes.data, buf.size, C.byref(n)))
+        return n.value
+
+    def trace_map(self, origins: np.ndarray, dirs: np.ndarray, max_steps: int) -> np.ndarray:
+        ctx = self.ctx
+        origins = np.ascontiguousarray(origins, np.float32).reshape(-1, 3)
+        dirs = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        n = origins.shape[0]
+        do, dd, dh = ctx.alloc(origins.nbytes), ctx.alloc(dirs.nbytes), ctx.alloc(max(n, 1) * 32)
+        try:
+            do.upload(origins)
+            dd.upload(dirs)
+            ctx.check(ctx.lib.vt_trace_map(ctx.handle, self.handle, do.ptr, dd.ptr, n, max_steps, dh.ptr, None))
+            ctx.sync()
+            return dh.download(np.zeros(n, REF_HIT_DTYPE))
+        finally:
+            do.free(), dd.free(), dh.free()
+
+    def render(self, cam: Camera_t) -> np.ndarray:
+        ctx = self.ctx
+        n = cam.width * cam.height
+        d = ctx.alloc(n * 32)
+        try:
+            ctx.check(ctx.lib.vt_render_reference(ctx.handle, self.handle, C.byref(cam), d.ptr, None))
+            ctx.sync()
+            return d.download(np.zeros(n, REF_PIXEL_DTYPE))
+        finally:
+            d.free()
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.vt_brickmap_destroy(self.handle)
+            self.handle = None
 
 
 class Batch:
