@@ -118,6 +118,9 @@ vt_status vt_world_upload_chunk(vt_world* world, int32_t cx, int32_t cy, int32_t
 /* VoxelBrickmap.set / get (voxel.zig:58-70): single voxel write/read. */
 vt_status vt_world_set_voxel(vt_world* world, int32_t x, int32_t y, int32_t z, uint8_t material, vt_stream stream);
 vt_status vt_world_get_voxel(vt_world* world, int32_t x, int32_t y, int32_t z, uint8_t* material);
+/* VoxelBrickmap.get (voxel.zig:63-70) over the whole grid: X*Y*Z bytes, x
+ * fastest, into host memory; returns after the copy has landed. */
+vt_status vt_world_download_dense(vt_world* world, uint8_t* h_materials, size_t nbytes, vt_stream stream);
 /* 256-entry RGBA8 palette (R in the low byte): albedo of each material in the
  * REFERENCE shading mode (the role of the model atlas texel, map.glsl:57-60). */
 vt_status vt_world_set_palette(vt_world* world, const uint32_t* h_rgba256);
@@ -393,6 +396,11 @@ void      vt_gen_desc_init(vt_gen_desc* desc, int32_t x, int32_t y, int32_t z, f
 vt_status vt_gen_world(const vt_gen_desc* desc, uint8_t* h_out, size_t nbytes, int32_t threads);
 /* Terrain height at column (x, z): cells y < height are solid before caves. */
 int32_t   vt_gen_height(const vt_gen_desc* desc, int32_t x, int32_t z);
+/* The same scene generated on the device straight into `world` (whose dims
+ * must equal desc->dims): the bytes equal vt_gen_world's.  Replaces the
+ * host procgen loop (procgen.zig:6-53) and the upload; asynchronous on
+ * `stream`. */
+vt_status vt_world_generate(vt_world* world, const vt_gen_desc* desc, vt_stream stream);
 /* A seeded pinhole camera camera_height above the terrain at a seeded column,
  * seeded yaw in [0, 360) degrees and pitch in [-30, 0] degrees, FOV 70 deg. */
 vt_status vt_gen_camera(const vt_gen_desc* desc, uint64_t seed, int32_t width, int32_t height, vt_camera* out);

@@ -68,6 +68,8 @@ def test_null_arguments_are_rejected(vtlib):
     assert lib.vt_world_destroy(None) == 1
     assert lib.vt_render(None, None, None, None, None, None) == 1
     assert lib.vt_gen_world(None, None, 0, 1) == 1
+    assert lib.vt_world_generate(None, None, None) == 1
+    assert lib.vt_world_download_dense(None, None, 0, None) == 1
 
 
 def test_generator_rejects_bad_sizes(vtlib):

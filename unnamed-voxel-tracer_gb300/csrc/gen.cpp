@@ -15,84 +15,11 @@
 #include <vector>
 
 #include "../../include/vt.h"
+#include "gen_noise.cuh"
 
 namespace {
 
-inline uint64_t mix64(uint64_t z) {
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-
-struct SplitMix {
-    uint64_t s;
-    uint64_t next() {
-        s += 0x9E3779B97F4A7C15ull;
-        return mix64(s);
-    }
-    double uniform() { return (double)(next() >> 11) * 0x1p-53; }
-};
-
-// Lattice value in [-1, 1).
-inline double lattice(uint64_t seed, int64_t x, int64_t y, int64_t z) {
-    uint64_t h = seed;
-    h = mix64(h ^ ((uint64_t)x * 0x9E3779B97F4A7C15ull));
-    h = mix64(h ^ ((uint64_t)y * 0xC2B2AE3D27D4EB4Full));
-    h = mix64(h ^ ((uint64_t)z * 0x165667B19E3779F9ull));
-    return (double)(h >> 11) * 0x1p-52 - 1.0;
-}
-
-inline double smooth(double t) { return t * t * (3.0 - 2.0 * t); }
-inline double lerp(double a, double b, double t) { return a + (b - a) * t; }
-
-double noise2(uint64_t seed, double x, double z) {
-    const double fx = floor(x), fz = floor(z);
-    const int64_t ix = (int64_t)fx, iz = (int64_t)fz;
-    const double sx = smooth(x - fx), sz = smooth(z - fz);
-    const double a = lerp(lattice(seed, ix, 0, iz), lattice(seed, ix + 1, 0, iz), sx);
-    const double b = lerp(lattice(seed, ix, 0, iz + 1), lattice(seed, ix + 1, 0, iz + 1), sx);
-    return lerp(a, b, sz);
-}
-
-double noise3(uint64_t seed, double x, double y, double z) {
-    const double fx = floor(x), fy = floor(y), fz = floor(z);
-    const int64_t ix = (int64_t)fx, iy = (int64_t)fy, iz = (int64_t)fz;
-    const double sx = smooth(x - fx), sy = smooth(y - fy), sz = smooth(z - fz);
-    double c[2][2];
-    for (int dz = 0; dz < 2; ++dz)
-        for (int dy = 0; dy < 2; ++dy)
-            c[dz][dy] = lerp(lattice(seed, ix, iy + dy, iz + dz), lattice(seed, ix + 1, iy + dy, iz + dz), sx);
-    return lerp(lerp(c[0][0], c[0][1], sy), lerp(c[1][0], c[1][1], sy), sz);
-}
-
-constexpr uint64_t kOctaveSalt = 0x632BE59BD9B4E019ull;
-
-double fbm2(uint64_t seed, double x, double z, double freq, int octaves) {
-    double sum = 0.0, amp = 1.0, norm = 0.0;
-    for (int o = 0; o < octaves; ++o) {
-        sum += amp * noise2(seed + (uint64_t)o * kOctaveSalt, x * freq, z * freq);
-        norm += amp;
-        amp *= 0.5;
-        freq *= 2.0;
-    }
-    return sum / norm;
-}
-
-double fbm3(uint64_t seed, double x, double y, double z, double freq) {
-    const double a = noise3(seed, x * freq, y * freq, z * freq);
-    const double b = noise3(seed + kOctaveSalt, x * freq * 2.0, y * freq * 2.0, z * freq * 2.0);
-    return (a + 0.5 * b) / 1.5;
-}
-
-uint64_t stream_seed(uint64_t seed, uint64_t purpose) { return mix64(seed ^ mix64(purpose)); }
-
-constexpr uint64_t kTerrain = 1, kCaves = 2, kTrees = 3, kLeaves = 4, kCamera = 5, kSun = 6;
-
-int height_at(const vt_gen_desc* d, int x, int z) {
-    const double f = fbm2(stream_seed(d->seed, kTerrain), (double)x, (double)z, 1.0 / (double)d->period, d->octaves);
-    int h = (int)floor((double)d->base_height + (double)d->amplitude * f);
-    return std::max(1, std::min(h, d->dims[1] - 1));
-}
+using namespace vt::gen;
 
 // Deterministic double sine/cosine: reduction by pi/2 split into
 // 0x1.921fb5p+0 + 0x1.110b46p-26 + 0x1.1a62633145c07p-54 (each the leading
@@ -132,44 +59,9 @@ void fill_slab(const vt_gen_desc* d, uint8_t* out, int z0, int z1) {
     for (int z = z0; z < z1; ++z)
         for (int x = 0; x < X; ++x) {
             const int h = height_at(d, x, z);
-            for (int y = 0; y < Y; ++y) {
-                uint8_t m = 0;
-                if (y < h) {
-                    m = (y == h - 1) ? 1 : (y >= h - 4 ? 2 : 3);
-                    if (d->caves && y > 0 && fbm3(cs, (double)x, (double)y, (double)z, cf) > (double)d->cave_threshold) m = 0;
-                } else if (y < water) {
-                    m = 4;
-                }
-                out[(size_t)x + (size_t)X * ((size_t)y + (size_t)Y * (size_t)z)] = m;
-            }
+            for (int y = 0; y < Y; ++y)
+                out[(size_t)x + (size_t)X * ((size_t)y + (size_t)Y * (size_t)z)] = cell_material(d, x, y, z, h, water, cs, cf);
         }
-}
-
-void plant_trees(const vt_gen_desc* d, uint8_t* out) {
-    const int X = d->dims[0], Y = d->dims[1], Z = d->dims[2];
-    if (X < 6 || Z < 6) return;
-    SplitMix rng{stream_seed(d->seed, kTrees)};
-    const uint64_t ls = stream_seed(d->seed, kLeaves);
-    auto at = [&](int x, int y, int z) -> uint8_t& {
-        return out[(size_t)x + (size_t)X * ((size_t)y + (size_t)Y * (size_t)z)];
-    };
-    for (int t = 0; t < d->trees; ++t) {
-        const int x = 2 + (int)(rng.uniform() * (double)(X - 4));
-        const int z = 2 + (int)(rng.uniform() * (double)(Z - 4));
-        const int h = height_at(d, x, z);
-        if (h + 8 >= Y) continue;
-        for (int y = h; y < h + 6; ++y) at(x, y, z) = 5;
-        for (int dz = -2; dz <= 2; ++dz)
-            for (int dy = -2; dy <= 2; ++dy)
-                for (int dx = -2; dx <= 2; ++dx) {
-                    const int lx = x + dx, ly = h + 5 + dy, lz = z + dz;
-                    if (lx < 0 || lz < 0 || lx >= X || lz >= Z || ly >= Y) continue;
-                    uint8_t& c = at(lx, ly, lz);
-                    if (c != 0 && c != 4) continue;
-                    const uint64_t hh = mix64(ls ^ mix64(((uint64_t)t << 20) ^ (uint64_t)((dx + 2) + 5 * ((dy + 2) + 5 * (dz + 2)))));
-                    if ((double)(hh >> 11) * 0x1p-53 < 0.7) c = 6;
-                }
-    }
 }
 
 }  // namespace

@@ -114,6 +114,9 @@ vt_status check_cuda(vt_ctx* ctx, cudaError_t err, const char* what);
 vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out);
 // Rebuilds the empty-space distances of a world on `st`.
 vt_status rebuild_distances(vt_world* w, cudaStream_t st);
+// The world's staging buffer, grown to at least `bytes` (synchronises the
+// device when it has to grow).
+vt_status world_stage(vt_world* w, size_t bytes, unsigned char** out);
 // Argument checks shared by the render entry points.
 vt_status check_frame_args(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p);
 // Queues one frame (render kernel, distances rebuilt first if stale) writing

@@ -153,8 +153,11 @@ vt_status rebuild_distances(vt_world* w, cudaStream_t st) {
     return VT_OK;
 }
 
-static vt_status ensure_stage(vt_world* w, size_t bytes) {
-    if (bytes <= w->stage_bytes) return VT_OK;
+vt_status world_stage(vt_world* w, size_t bytes, unsigned char** out) {
+    if (bytes <= w->stage_bytes) {
+        *out = w->d_stage;
+        return VT_OK;
+    }
     if (w->d_stage) {
         VT_CUDA(w->ctx, cudaDeviceSynchronize());
         cudaFree(w->d_stage);
@@ -163,6 +166,7 @@ static vt_status ensure_stage(vt_world* w, size_t bytes) {
     }
     VT_CUDA(w->ctx, cudaMalloc(&w->d_stage, bytes));
     w->stage_bytes = bytes;
+    *out = w->d_stage;
     return VT_OK;
 }
 
@@ -248,7 +252,8 @@ vt_status vt_world_upload_dense(vt_world* w, const uint8_t* h_materials, size_t 
     if (!w) return VT_ERR_ARG;
     const size_t need = (size_t)w->dims[0] * w->dims[1] * w->dims[2];
     if (!h_materials || nbytes != need) return fail(w->ctx, VT_ERR_ARG, "dense upload needs exactly X*Y*Z bytes");
-    vt_status s = ensure_stage(w, need);
+    unsigned char* stage = nullptr;
+    vt_status s = world_stage(w, need, &stage);
     if (s) return s;
     cudaStream_t st = (cudaStream_t)stream;
     VT_CUDA(w->ctx, cudaMemcpyAsync(w->d_stage, h_materials, need, cudaMemcpyHostToDevice, st));
@@ -269,7 +274,8 @@ vt_status vt_world_upload_chunk(vt_world* w, int32_t cx, int32_t cy, int32_t cz,
     if (!h_chunk) return fail(w->ctx, VT_ERR_ARG, "null chunk");
     if (cx < 0 || cy < 0 || cz < 0 || cx >= w->cdim[0] || cy >= w->cdim[1] || cz >= w->cdim[2])
         return fail(w->ctx, VT_ERR_ARG, "chunk coordinate out of range");
-    vt_status s = ensure_stage(w, kChunkBytes);
+    unsigned char* stage = nullptr;
+    vt_status s = world_stage(w, kChunkBytes, &stage);
     if (s) return s;
     cudaStream_t st = (cudaStream_t)stream;
     VT_CUDA(w->ctx, cudaMemcpyAsync(w->d_stage, h_chunk, kChunkBytes, cudaMemcpyHostToDevice, st));

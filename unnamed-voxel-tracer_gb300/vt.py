@@ -122,6 +122,7 @@ _SIGNATURES = {
     "vt_world_upload_chunk": (_S, [_P, C.c_int32, C.c_int32, C.c_int32, _P, _P]),
     "vt_world_set_voxel": (_S, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_uint8, _P]),
     "vt_world_get_voxel": (_S, [_P, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_uint8)]),
+    "vt_world_download_dense": (_S, [_P, _P, C.c_size_t, _P]),
     "vt_world_set_palette": (_S, [_P, _P]),
     "vt_world_get_info": (_S, [_P, C.POINTER(WorldInfo_t)]),
     "vt_camera_look": (_S, [C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float, C.c_int32, C.c_int32,
@@ -153,6 +154,7 @@ _SIGNATURES = {
     "vt_gen_desc_init": (None, [C.POINTER(GenDesc_t), C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64]),
     "vt_gen_world": (_S, [C.POINTER(GenDesc_t), _P, C.c_size_t, C.c_int32]),
     "vt_gen_height": (C.c_int32, [C.POINTER(GenDesc_t), C.c_int32, C.c_int32]),
+    "vt_world_generate": (_S, [_P, C.POINTER(GenDesc_t), _P]),
     "vt_gen_camera": (_S, [C.POINTER(GenDesc_t), C.c_uint64, C.c_int32, C.c_int32, C.POINTER(Camera_t)]),
     "vt_default_palette": (_S, [_P]),
     "vt_gen_sun": (_S, [C.c_uint64, C.POINTER(C.c_float)]),
@@ -325,6 +327,17 @@ class World:
         m = C.c_uint8()
         self.ctx.check(self.ctx.lib.vt_world_get_voxel(self.handle, x, y, z, C.byref(m)))
         return int(m.value)
+
+    def download_dense(self, stream=None) -> np.ndarray:
+        """The whole grid as a uint8 array indexed [z, y, x]."""
+        X, Y, Z = self.dims
+        out = np.empty((Z, Y, X), dtype=np.uint8)
+        self.ctx.check(self.ctx.lib.vt_world_download_dense(self.handle, _ptr(out), out.nbytes, stream))
+        return out
+
+    def generate(self, desc: "GenDesc_t", stream=None) -> None:
+        """Generates the scene `desc` on the device (same bytes as gen_world)."""
+        self.ctx.check(self.ctx.lib.vt_world_generate(self.handle, C.byref(desc), stream))
 
     def clear(self, stream=None) -> None:
         self.ctx.check(self.ctx.lib.vt_world_clear(self.handle, stream))
