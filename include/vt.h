@@ -289,6 +289,18 @@ vt_status vt_trace_map(vt_ctx* ctx, const vt_brickmap* bm, const float* d_origin
  * vt_ref_pixel records on the device.  Rows are the GL image's rows. */
 vt_status vt_render_reference(vt_ctx* ctx, const vt_brickmap* bm, const vt_camera* cam, vt_ref_pixel* d_out,
                               vt_stream stream);
+/* VoxelBrickmap.get over the whole map (voxel.zig:63-70): the chunk table
+ * (64^3 u32) and the first nbricks bricks (512 u32 each) back to the host,
+ * after all work queued on the device. */
+vt_status vt_brickmap_download(vt_brickmap* bm, uint32_t* h_chunks, uint32_t* h_bricks, size_t nbricks);
+/* The editing pass (terrain_edit.comp.glsl:11-24): the pick ray through the
+ * view centre traced with 64 steps, then, on a hit, edit_mode > 0 writes
+ * Voxel{ty = edit_mode - 1, is_solid = 1} into the voxel in front of the hit
+ * face and edit_mode == 0 clears the hit voxel, through map_setVoxel
+ * (map.glsl:49-55: dropped where the chunk has no brick).  edit_mode == -1
+ * only picks.  d_out (NULL allowed): one vt_ref_hit.  Asynchronous. */
+vt_status vt_brickmap_edit(vt_ctx* ctx, vt_brickmap* bm, const vt_camera* cam, int32_t edit_mode, vt_ref_hit* d_out,
+                           vt_stream stream);
 
 /* ----------------------------------------------------------------- batch
  * Many scenes x cameras in one launch (no counterpart in the reference, which
@@ -372,6 +384,27 @@ vt_status vt_autotune(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, 
 vt_status vt_trace_rays(vt_ctx* ctx, const vt_world* world, const float* d_origins,
                         const float* d_dirs, int32_t n, int32_t max_steps,
                         vt_hit* d_out, vt_stream stream);
+
+/* ------------------------------------------------------------ pick / edit
+ * The pick ray of terrain_edit.comp.glsl:11-17 on the mode-P world: the
+ * camera's ray of UV (0, 0), i.e. the primary ray of pixel (W/2, H/2) for
+ * even W and H, traced with max_steps.  vt_pick returns its hit record to the
+ * host (synchronous, on the context's stream). */
+vt_status vt_pick(vt_ctx* ctx, vt_world* world, const vt_camera* cam, int32_t max_steps, vt_hit* h_out);
+/* Pick and edit in one launch, nothing read back (terrain_edit.comp.glsl:
+ * 19-24 on the mode-P world): on a hit, edit_mode 0 clears the hit voxel and
+ * edit_mode 1..255 writes that material into the voxel in front of the hit
+ * face (skipped outside the world); -1 only picks.  The brick word, chunk bit
+ * and the empty-space distances around the voxel are updated on `stream`.
+ * d_out (NULL allowed) receives the pick's vt_hit.  Edits on one world are
+ * serialised by the caller (one stream per world). */
+vt_status vt_edit(vt_ctx* ctx, vt_world* world, const vt_camera* cam, int32_t max_steps, int32_t edit_mode,
+                  vt_hit* d_out, vt_stream stream);
+/* The empty-space distances the traversal skips by (brought up to date
+ * first): one byte per brick (chunk-major, 512 per chunk, brick bx + 8*(by +
+ * 8*bz)) and one per chunk.  For tests and tools. */
+vt_status vt_world_download_distances(vt_world* world, uint8_t* h_brick, size_t brick_bytes, uint8_t* h_chunk,
+                                      size_t chunk_bytes);
 
 /* ------------------------------------------------------------- generators
  * Seeded synthetic scenes (host code, deterministic across machines). */

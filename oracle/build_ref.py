@@ -9,6 +9,7 @@ Reads the reference's GLSL where it lies (REFERENCE_ROOT, default
                    the SSBO/image declarations are replaced by ref_shim.cpp
   ref_camera.inc   camera.glsl after the uniform block (SUN_DIR, SkyDome2)
   ref_primary.inc  primary.comp.glsl from `vec2 rayUV` to the traceMap call
+  ref_edit.inc     terrain_edit.comp.glsl, the same span (the pick ray)
 
 Two mechanical rewrites make GLSL parse as C++ with GLSL's float semantics:
 float literals get an `f` suffix (GLSL literals are single precision) and the
@@ -59,21 +60,24 @@ def extract_primary(text: str) -> str:
     return "\n".join(lines[start:end + 1]) + "\n"
 
 
+SOURCES = ("map.glsl", "camera.glsl", "primary.comp.glsl", "terrain_edit.comp.glsl")
+
+
 def available() -> bool:
-    return all((SHADERS / f).exists() for f in ("map.glsl", "camera.glsl", "primary.comp.glsl"))
+    return all((SHADERS / f).exists() for f in SOURCES)
 
 
 def build(force: bool = False) -> Path:
     if not available():
         raise FileNotFoundError(f"reference shaders not found under {SHADERS}")
-    deps = [SHADERS / "map.glsl", SHADERS / "camera.glsl", SHADERS / "primary.comp.glsl", HERE / "ref_shim.cpp",
-            HERE / "glsl_compat.hpp", Path(__file__)]
+    deps = [SHADERS / f for f in SOURCES] + [HERE / "ref_shim.cpp", HERE / "glsl_compat.hpp", Path(__file__)]
     if not force and LIB.exists() and all(d.stat().st_mtime <= LIB.stat().st_mtime for d in deps):
         return LIB
     OUT.mkdir(exist_ok=True)
     (OUT / "ref_map.inc").write_text(to_cpp(extract_map((SHADERS / "map.glsl").read_text())))
     (OUT / "ref_camera.inc").write_text(to_cpp(extract_camera((SHADERS / "camera.glsl").read_text())))
     (OUT / "ref_primary.inc").write_text(to_cpp(extract_primary((SHADERS / "primary.comp.glsl").read_text())))
+    (OUT / "ref_edit.inc").write_text(to_cpp(extract_primary((SHADERS / "terrain_edit.comp.glsl").read_text())))
     tmp = LIB.with_suffix(".so.tmp")
     cmd = ["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-w",
            "-I", str(HERE), "-I", str(OUT), str(HERE / "ref_shim.cpp"), "-o", str(tmp)]

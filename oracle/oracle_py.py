@@ -80,6 +80,10 @@ def load() -> C.CDLL:
         lib.vto_sky_ref.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float)]
         lib.vto_render_reference.argtypes = [C.POINTER(VtoRefWorld_t), C.POINTER(C.c_float),
                                              C.POINTER(C.c_float), C.c_float, C.c_int32, C.c_int32, P]
+        lib.vto_edit_r.argtypes = [C.POINTER(VtoRefWorld_t), P, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                   C.c_int32, C.POINTER(VtoRefHit_t)]
+        lib.vto_pick_p.argtypes = [C.POINTER(VtoWorld_t), C.POINTER(vt.Camera_t), C.c_int32, C.c_int32,
+                                   C.POINTER(VtoTrace_t), C.POINTER(C.c_int32)]
         _lib = lib
     return _lib
 
@@ -146,6 +150,22 @@ def tracemap(world: OracleRefWorld, o, d, max_steps: int) -> VtoRefHit_t:
     h = VtoRefHit_t()
     load().vto_tracemap(C.byref(world.w), (C.c_float * 3)(*o), (C.c_float * 3)(*d), max_steps, C.byref(h))
     return h
+
+
+def edit_r(world: OracleRefWorld, cam, edit_mode: int) -> VtoRefHit_t:
+    """The editing pass on the reference world; writes into world.data."""
+    h = VtoRefHit_t()
+    load().vto_edit_r(C.byref(world.w), world.data.ctypes.data, (C.c_float * 4)(*cam.pos),
+                      (C.c_float * 16)(*cam.view), edit_mode, C.byref(h))
+    return h
+
+
+def pick_p(world: OracleWorld, cam, max_steps: int, edit_mode: int = -1):
+    """(trace, target {x, y, z, valid}) of the mode-P pick ray."""
+    tr = VtoTrace_t()
+    tgt = (C.c_int32 * 4)()
+    load().vto_pick_p(C.byref(world.w), C.byref(cam), max_steps, edit_mode, C.byref(tr), tgt)
+    return tr, list(tgt)
 
 
 def shade_grad_f64(world: OracleWorld, cam, hits: np.ndarray, palette, albedo, sun, ambient: float, diffuse: float,
@@ -230,5 +250,7 @@ def load_ref():
         lib.ref_sky.argtypes = [F, F, F]
         lib.ref_primary.argtypes = [F, F, C.c_float, C.c_int32, C.c_int32, C.c_int32, C.c_int32, F,
                                     C.POINTER(C.c_uint32), F, F]
+        lib.ref_pick.argtypes = [F, F, C.POINTER(C.c_uint32), F, F]
+        lib.ref_set_voxel.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_uint32]
         _ref = lib
     return _ref

@@ -68,4 +68,15 @@ void ref_primary(const float cam_pos[4], const float view[16], float cam_fov, in
     put(inter, out_data, hit_pos, normal);
 }
 
+// terrain_edit.comp.glsl:11-17 (the pick ray) and map_setVoxel
+// (map.glsl:49-55), the two pieces of the reference's editing pass.
+void ref_pick(const float cam_pos[4], const float view[16], uint32_t* out_data, float hit_pos[3], float normal[3]) {
+    C_position = vec4(cam_pos[0], cam_pos[1], cam_pos[2], cam_pos[3]);
+    for (int i = 0; i < 16; ++i) C_view.m[i] = view[i];
+#include "ref_edit.inc"
+    put(inter, out_data, hit_pos, normal);
+}
+
+void ref_set_voxel(int32_t x, int32_t y, int32_t z, uint32_t voxel) { map_setVoxel(ivec3(x, y, z), voxel); }
+
 }  // extern "C"

@@ -723,14 +723,9 @@ void vto_tracemap(const vto_refworld* w, const float o[3], const float din[3], i
 static float fmin_g(float a, float b) { return b < a ? b : a; }
 static float fmax_g(float a, float b) { return a < b ? b : a; }
 
-void vto_primary_r(const vto_refworld* w, const float cam_pos[4], const float view[16], float fov, int32_t px,
-                   int32_t py, int32_t width, int32_t height, int32_t max_steps, float dir_out[3], vto_refhit* out) {
-    float ux = (float)px / (float)width * 2.0f - 1.0f;
-    float uy = (float)py / (float)height * 2.0f - 1.0f;
-    uy *= (float)height / (float)width;
-    const float th = tanf(fov / 2.0f);
-    ux *= th;
-    uy *= th;
+/* primary.comp.glsl:38-43 from the final ray UV (fov factor applied). */
+static void ray_r(const vto_refworld* w, const float cam_pos[4], const float view[16], float ux, float uy,
+                  int32_t max_steps, float dir_out[3], vto_refhit* out) {
     const float v[4] = {ux, uy, 1.0f, 1.0f};
     float q[4];
     for (int i = 0; i < 4; ++i)
@@ -752,6 +747,68 @@ void vto_primary_r(const vto_refworld* w, const float cam_pos[4], const float vi
     for (int i = 0; i < 3; ++i) start[i] = (o[i] + d[i] * s) - 0.001f;
     for (int i = 0; i < 3; ++i) dir_out[i] = d[i];
     vto_tracemap(w, start, d, max_steps, out);
+}
+
+void vto_primary_r(const vto_refworld* w, const float cam_pos[4], const float view[16], float fov, int32_t px,
+                   int32_t py, int32_t width, int32_t height, int32_t max_steps, float dir_out[3], vto_refhit* out) {
+    float ux = (float)px / (float)width * 2.0f - 1.0f;
+    float uy = (float)py / (float)height * 2.0f - 1.0f;
+    uy *= (float)height / (float)width;
+    const float th = tanf(fov / 2.0f);
+    ux *= th;
+    uy *= th;
+    ray_r(w, cam_pos, view, ux, uy, max_steps, dir_out, out);
+}
+
+/* terrain_edit.comp.glsl:11-17 (the pick: UV 0, no fov factor, 64 steps) and
+ * the edit of its commented-out tail (:19-24) through map_setVoxel
+ * (map.glsl:49-55): place Voxel{ty = edit_mode - 1, is_solid} at
+ * ivec3(hit_pos + normal) >> 3, or clear ivec3(hit_pos) >> 3; the write is
+ * dropped where the chunk has no brick (and beyond the pool). */
+void vto_edit_r(const vto_refworld* w, uint32_t* data, const float cam_pos[4], const float view[16],
+                int32_t edit_mode, vto_refhit* out) {
+    float dir[3];
+    ray_r(w, cam_pos, view, 0.0f, 0.0f, 64, dir, out);
+    if (edit_mode < 0 || out->data == 0) return;
+    int p[3];
+    uint32_t voxel;
+    for (int i = 0; i < 3; ++i)
+        p[i] = edit_mode > 0 ? ((int)(out->hit_pos[i] + out->normal[i])) >> 3 : ((int)out->hit_pos[i]) >> 3;
+    voxel = edit_mode > 0 ? (1u << 28) + (uint32_t)edit_mode - 1u : 0u;
+    const int cx = p[0] >> 3, cy = p[1] >> 3, cz = p[2] >> 3;
+    if (cx < 0 || cy < 0 || cz < 0 || cx >= 64 || cy >= 64 || cz >= 64) return;
+    const uint32_t blk = w->chunks[cx + 64 * (cy + 64 * cz)];
+    if (blk == 0) return;
+    const uint64_t idx = (uint64_t)(blk - 1) * 512u + (uint64_t)((p[0] % 8) + ((p[2] % 8) * 8 + (p[1] % 8)) * 8);
+    if (idx < w->ndata) data[idx] = voxel;
+}
+
+/* The pick ray of terrain_edit.comp.glsl:11-17 on the mode-P world: the
+ * primary ray of UV (0, 0) traced with max_steps; target = {x, y, z, valid}
+ * of the voxel an edit with edit_mode would write (0: the hit voxel; > 0: the
+ * voxel in front of the hit face, invalid outside the world; < 0: none). */
+void vto_pick_p(const vto_world* w, const vt_camera* cam, int32_t max_steps, int32_t edit_mode, vto_trace* out,
+                int32_t target[4]) {
+    const float u = 0.0f, v = 0.0f;
+    const float* M = cam->view;
+    float q[3], o[3], d[3];
+    for (int j = 0; j < 3; ++j) q[j] = ((u * M[0 * 4 + j] + v * M[1 * 4 + j]) + M[2 * 4 + j]) + M[3 * 4 + j];
+    const float len = sqrtf((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]);
+    for (int j = 0; j < 3; ++j) {
+        d[j] = q[j] / len;
+        o[j] = cam->pos[j];
+    }
+    vto_trace_p(w, o, d, max_steps, out);
+    target[0] = target[1] = target[2] = target[3] = 0;
+    if (!out->hit || edit_mode < 0) return;
+    int c[3] = {out->cell[0], out->cell[1], out->cell[2]};
+    if (edit_mode > 0) c[out->axis] += (out->face & 1) ? 1 : -1; /* face 2a: +dir (step back -1); 2a+1: -dir */
+    for (int i = 0; i < 3; ++i)
+        if (c[i] < 0 || c[i] >= w->dims[i]) return;
+    target[0] = c[0];
+    target[1] = c[1];
+    target[2] = c[2];
+    target[3] = 1;
 }
 
 /* ---------------------------------------------------------------------

@@ -61,6 +61,11 @@ typedef struct {
 /* One mode-P ray, unit stepping. */
 void vto_trace_p(const vto_world* w, const float o[3], const float d[3], int32_t max_steps, vto_trace* out);
 
+/* The pick ray (terrain_edit.comp.glsl:11-17) on the mode-P world and the
+ * voxel {x, y, z, valid} an edit with edit_mode writes. */
+void vto_pick_p(const vto_world* w, const vt_camera* cam, int32_t max_steps, int32_t edit_mode, vto_trace* out,
+                int32_t target[4]);
+
 /* Shading + ray generation for pixel rows [y0, y1) of a frame. */
 void vto_render_rows(const vto_world* w, const uint32_t* palette, const vt_camera* cam,
                      const vt_params* p, vt_hit* out, int32_t y0, int32_t y1, vt_stats* st);
@@ -114,6 +119,11 @@ void vto_tracemap(const vto_refworld* w, const float o[3], const float d[3], int
  * map box and traced with traceMap(..., max_steps). */
 void vto_primary_r(const vto_refworld* w, const float cam_pos[4], const float view[16], float fov, int32_t px,
                    int32_t py, int32_t width, int32_t height, int32_t max_steps, float dir_out[3], vto_refhit* out);
+
+/* The editing pass (terrain_edit.comp.glsl:11-24): pick (UV 0, 64 steps) and
+ * map_setVoxel into `data` (the pool w->data points to, writable). */
+void vto_edit_r(const vto_refworld* w, uint32_t* data, const float cam_pos[4], const float view[16],
+                int32_t edit_mode, vto_refhit* out);
 
 /* traceEntities (map.glsl:172-201, the part that runs: five unit boxes, the
  * sentinel 0xFFFFFFFF on a hit). */

@@ -6,6 +6,8 @@ they are not).
                      (map.glsl:83-168 compiled as C++ by oracle/build_ref.py),
                      on a seeded world in the reference's format
   ref_primary.npz    the reference's primary rays and hits (primary.comp.glsl:31-43)
+  ref_edit.npz       a sequence of editing passes (terrain_edit.comp.glsl's pick
+                     ray, then map_setVoxel) and the brick pool after each
   oracle_frames.json hashes of the mode-P oracle's records for fixed seeds
 
     python tests/golden/make_golden.py
@@ -54,6 +56,45 @@ def golden_rays():
 def golden_camera():
     desc = vt.gen_desc((96, 80, 112), scale=0.5, seed=WORLD_SEED)
     return vt.gen_camera(desc, 3, 64, 48)
+
+
+N_EDITS = 48
+
+
+def edit_sequence():
+    """(camera, edit_mode) pairs of the editing fixture: cameras over the golden
+    world, edit_mode -1 (pick only), 0 (clear) or 1..29 (place model)."""
+    desc = vt.gen_desc((96, 80, 112), scale=0.5, seed=WORLD_SEED)
+    rng = np.random.default_rng(WORLD_SEED + 2)
+    seq = []
+    for i in range(N_EDITS):
+        cam = vt.gen_camera(desc, 100 + i, 2, 2)
+        seq.append((cam, int(rng.choice([-1, 0, 0, 1, 5, 13, 29]))))
+    return seq
+
+
+def ref_edit_run(ref, chunks, data, atlas):
+    """Runs edit_sequence on the compiled reference: its pick (terrain_edit.comp
+    .glsl:11-17) and its map_setVoxel (map.glsl:49-55), with the placement of
+    the commented-out tail (:19-24).  Writes into `data`."""
+    ref.ref_set_world(chunks.ctypes.data, data.ctypes.data, atlas.ctypes.data)
+    out = {"data": [], "hit_pos": [], "normal": [], "pool_sha256": []}
+    for cam, mode in edit_sequence():
+        v, hp, nm = C.c_uint32(), (C.c_float * 3)(), (C.c_float * 3)()
+        ref.ref_pick((C.c_float * 4)(*cam.pos), (C.c_float * 16)(*cam.view), C.byref(v), hp, nm)
+        if v.value != 0 and mode >= 0:
+            h = np.array(list(hp), np.float32)
+            if mode > 0:
+                p = [int(x) >> 3 for x in (h + np.array(list(nm), np.float32))]
+                ref.ref_set_voxel(p[0], p[1], p[2], (1 << 28) + mode - 1)
+            else:
+                p = [int(x) >> 3 for x in h]
+                ref.ref_set_voxel(p[0], p[1], p[2], 0)
+        out["data"].append(v.value)
+        out["hit_pos"].append(list(hp))
+        out["normal"].append(list(nm))
+        out["pool_sha256"].append(hashlib.sha256(data.tobytes()).hexdigest())
+    return out
 
 
 def frame_hash(records: np.ndarray) -> str:
@@ -115,6 +156,12 @@ def main() -> None:
                             C.byref(v), h3, n3)
             dirs[py, px], data_p[py, px], hp[py, px], nm[py, px] = list(d3), v.value, list(h3), list(n3)
     np.savez_compressed(HERE / "ref_primary.npz", dir=dirs, data=data_p, hit_pos=hp, normal=nm)
+
+    _, _, chunks, data, atlas = golden_world()
+    ed = ref_edit_run(ref, chunks, data.copy(), atlas)
+    np.savez_compressed(HERE / "ref_edit.npz", data=np.array(ed["data"], np.uint32),
+                        hit_pos=np.array(ed["hit_pos"], np.float32), normal=np.array(ed["normal"], np.float32),
+                        pool_sha256=np.array(ed["pool_sha256"]))
 
     (HERE / "oracle_frames.json").write_text(json.dumps(oracle_frames(), indent=1, sort_keys=True) + "\n")
     print("fixtures written")

@@ -1,0 +1,166 @@
+"""Pick and edit on the device against the oracle, and the incremental
+empty-space distance updates against a full rebuild.
+
+Bar: pick hit records bit-exact; the world after every edit byte-identical
+to the oracle's simulation; distances after any sequence of edits equal to
+those of a fresh upload of the same bytes (brick and chunk level); the
+mode-R editing pass bit-exact against the oracle's restatement (pinned to
+the reference by test_oracle_edit)."""
+import hashlib
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+import make_golden as G  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def fresh_distances(vt, ctx, mats):
+    Z, Y, X = mats.shape
+    w = vt.World(ctx, (X, Y, Z))
+    try:
+        w.upload_dense(mats)
+        return w.distances()
+    finally:
+        w.close()
+
+
+def assert_same_distances(vt, ctx, world, mats):
+    b, c = world.distances()
+    fb, fc = fresh_distances(vt, ctx, mats)
+    assert np.array_equal(c, fc)
+    bad = np.flatnonzero(b != fb)
+    assert bad.size == 0, (bad[:8], b[bad[:8]], fb[bad[:8]])
+
+
+def test_pick_matches_oracle(vt, oracle, ctx):
+    desc = vt.gen_desc((160, 96, 128), scale=0.6, seed=4, trees=40, caves=True)
+    mats = vt.gen_world(desc)
+    ow = oracle.OracleWorld(mats)
+    w = vt.World(ctx, (160, 96, 128))
+    try:
+        w.upload_dense(mats)
+        hits = 0
+        for s in range(24):
+            cam = vt.gen_camera(desc, s, 64, 48)
+            for steps in (40, 1000):
+                h = w.pick(cam, steps)
+                tr, _ = oracle.pick_p(ow, cam, steps)
+                if tr.hit:
+                    hits += 1
+                    assert h["voxel"] == tr.voxel and h["face"] == tr.face and h["material"] == tr.material
+                    assert np.float32(tr.t).view(np.uint32) == h["t"].view(np.uint32)
+                else:
+                    assert h["face"] == 0xFF and h["voxel"] == 0xFFFFFFFF
+        assert hits > 10
+    finally:
+        w.close()
+
+
+def test_edit_sequence_matches_oracle_and_distances_stay_exact(vt, oracle, ctx):
+    desc = vt.gen_desc((128, 96, 160), scale=0.6, seed=12, trees=30)
+    mats = vt.gen_world(desc)
+    rng = np.random.default_rng(12)
+    w = vt.World(ctx, (128, 96, 160))
+    hit_buf = ctx.alloc(16)
+    try:
+        w.upload_dense(mats)
+        w.pick(vt.gen_camera(desc, 0, 8, 8), 10)         # builds the distances once
+        changed = 0
+        for i in range(60):
+            cam = vt.gen_camera(desc, 1000 + i % 20, 8, 8)   # cameras repeat: digging into the same spot
+            mode = int(rng.choice([0, 0, 0, 1, 6, 200]))
+            tr, tgt = oracle.pick_p(oracle.OracleWorld(mats), cam, 600, edit_mode=mode)
+            w.edit(cam, 600, mode, d_out=hit_buf)
+            got = hit_buf.download(np.zeros(1, vt.HIT_DTYPE))[0]
+            assert got["voxel"] == (tr.voxel if tr.hit else 0xFFFFFFFF)
+            if tgt[3]:
+                x, y, z = tgt[:3]
+                changed += mats[z, y, x] != mode
+                mats[z, y, x] = mode
+            if i % 15 == 14:
+                assert np.array_equal(w.download_dense(), mats)
+                assert_same_distances(vt, ctx, w, mats)
+        assert changed > 20
+    finally:
+        hit_buf.free()
+        w.close()
+
+
+def test_host_edits_update_distances_incrementally(vt, ctx):
+    rng = np.random.default_rng(9)
+    X, Y, Z = 200, 72, 136
+    mats = np.zeros((Z, Y, X), np.uint8)
+    mats[:20] = 3                                     # a floor
+    w = vt.World(ctx, (X, Y, Z))
+    try:
+        w.upload_dense(mats)
+        w.distances()
+        for rnd in range(4):
+            # scattered single voxels, a cleared chunk, a filled chunk
+            for _ in range(40):
+                x, y, z = rng.integers(0, X), rng.integers(0, Y), rng.integers(0, Z)
+                m = int(rng.choice([0, 7]))
+                w.set(int(x), int(y), int(z), m)
+                mats[z, y, x] = m
+            cx, cy, cz = rng.integers(0, X // 32), rng.integers(0, Y // 32), rng.integers(0, Z // 32)
+            chunk = (rng.random((32, 32, 32)) < (0.0 if rnd % 2 else 0.3)).astype(np.uint8) * 5
+            w.upload_chunk(int(cx), int(cy), int(cz), chunk)
+            sl = (slice(cz * 32, cz * 32 + 32), slice(cy * 32, cy * 32 + 32), slice(cx * 32, cx * 32 + 32))
+            mats[sl] = chunk[:mats[sl].shape[0], :mats[sl].shape[1], :mats[sl].shape[2]]
+            assert_same_distances(vt, ctx, w, mats)
+        # clearing the whole floor voxel by voxel in one column range empties chunks
+        for x in range(0, 32):
+            for z in range(0, 8):
+                for y in range(0, 20):
+                    w.set(x, y, z, 0)
+        mats[0:8, 0:20, 0:32] = 0
+        assert_same_distances(vt, ctx, w, mats)
+    finally:
+        w.close()
+
+
+def test_edited_world_renders_like_fresh_upload(vt, oracle, ctx):
+    desc = vt.gen_desc((96, 80, 112), scale=0.5, seed=31, trees=20)
+    mats = vt.gen_world(desc)
+    w = vt.World(ctx, (96, 80, 112))
+    try:
+        w.upload_dense(mats)
+        cam = vt.gen_camera(desc, 2, 128, 96)
+        p = vt.default_params()
+        vt.render_host(ctx, w, cam, p)
+        for i in range(30):
+            w.edit(vt.gen_camera(desc, 500 + i % 6, 8, 8), 500, 0 if i % 3 else 9)
+        got = vt.render_host(ctx, w, cam, p)
+        now = w.download_dense()
+        ref, _ = oracle.render(oracle.OracleWorld(now), vt.default_palette(), cam, p, threads=8)
+        for f in ("voxel", "face", "material", "flags"):
+            assert np.array_equal(got[f], ref[f]), f
+        assert not np.array_equal(now, mats)
+    finally:
+        w.close()
+
+
+def test_brickmap_edit_matches_oracle(vt, oracle, ctx):
+    _, _, chunks, data, atlas = G.golden_world()
+    bm = vt.Brickmap(ctx)
+    rw = oracle.OracleRefWorld(chunks, data.copy(), atlas)
+    try:
+        bm.upload(chunks, data)
+        bm.set_atlas(atlas, 8)
+        g = np.load(Path(__file__).resolve().parent / "golden" / "ref_edit.npz")
+        for i, (cam, mode) in enumerate(G.edit_sequence()):
+            h = bm.edit(cam, mode)
+            o = oracle.edit_r(rw, cam, mode)
+            assert h["data"] == o.data == g["data"][i], i
+            assert np.array_equal(h["hit_pos"].view(np.uint32), np.array(o.hit_pos, np.float32).view(np.uint32))
+            assert np.array_equal(h["normal"], np.array(o.normal, np.float32))
+        _, pool = bm.download(data.size // 512)
+        assert np.array_equal(pool, rw.data)
+        assert hashlib.sha256(pool.tobytes()).hexdigest() == g["pool_sha256"][-1]
+    finally:
+        bm.close()

@@ -210,8 +210,8 @@ vt_status launch_shade(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
         return fail(ctx, VT_ERR_ARG, "camera size out of range (1..32768)");
     const float len2 = (in->sun[0] * in->sun[0] + in->sun[1] * in->sun[1]) + in->sun[2] * in->sun[2];
     if (!(len2 > 0.0f)) return fail(ctx, VT_ERR_ARG, "sun direction must be nonzero");
-    if (world->dist_dirty) {
-        vt_status s = rebuild_distances(const_cast<vt_world*>(world), st);
+    {
+        vt_status s = update_distances(const_cast<vt_world*>(world), st);
         if (s) return s;
     }
     vt_params p;

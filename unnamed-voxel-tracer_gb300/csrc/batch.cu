@@ -134,11 +134,10 @@ vt_status vt_batch_launch(vt_batch* b, vt_stream stream) {
     vt_ctx* ctx = b->ctx;
     cudaStream_t st = (cudaStream_t)stream;
     // stale empty-space distances are rebuilt before (outside) the graph
-    for (const vt_world* w : b->worlds)
-        if (w->dist_dirty) {
-            vt_status s = rebuild_distances(const_cast<vt_world*>(w), st);
-            if (s) return s;
-        }
+    for (const vt_world* w : b->worlds) {
+        vt_status s = update_distances(const_cast<vt_world*>(w), st);
+        if (s) return s;
+    }
     if (!b->exec) {
         // capture on a private stream: the legacy default stream cannot be captured
         cudaStream_t cap = nullptr;

@@ -237,11 +237,9 @@ struct RefFrame {
     int width, height;
 };
 
-// primary.comp.glsl:31-43.
-__device__ void primary_ref(const RefView& w, const RefFrame& f, int px, int py, float dir[3], RefHit& h) {
-    float ux = (float)px / (float)f.width * 2.0f - 1.0f;
-    float uy = (float)py / (float)f.height * 2.0f - 1.0f;
-    uy *= (float)f.height / (float)f.width;
+// primary.comp.glsl:35-43 from the scaled ray UV (before the fov factor):
+// the view ray, clipped to the map box and traced with `steps`.
+__device__ void ray_ref(const RefView& w, const RefFrame& f, float ux, float uy, int steps, float dir[3], RefHit& h) {
     ux *= f.tan_half;
     uy *= f.tan_half;
     const float v[4] = {ux, uy, 1.0f, 1.0f};
@@ -267,7 +265,48 @@ __device__ void primary_ref(const RefView& w, const RefFrame& f, int px, int py,
     float start[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) start[i] = (o[i] + dir[i] * s) - 0.001f;
-    trace_map(w, start, dir, 192, h);
+    trace_map(w, start, dir, steps, h);
+}
+
+// primary.comp.glsl:31-43.
+__device__ void primary_ref(const RefView& w, const RefFrame& f, int px, int py, float dir[3], RefHit& h) {
+    const float ux = (float)px / (float)f.width * 2.0f - 1.0f;
+    float uy = (float)py / (float)f.height * 2.0f - 1.0f;
+    uy *= (float)f.height / (float)f.width;
+    ray_ref(w, f, ux, uy, 192, dir, h);
+}
+
+// terrain_edit.comp.glsl:11-17: the pick ray through the view centre (UV 0),
+// traced with 64 steps; then the edit its commented-out tail describes
+// (:19-24): edit_mode > 0 writes Voxel{ty = edit_mode - 1, is_solid} in
+// front of the hit face, edit_mode == 0 clears the hit voxel, both through
+// map_setVoxel (map.glsl:49-55), which drops writes into chunks without a
+// brick.  edit_mode < 0 only picks.  One thread.
+__global__ void k_brickmap_edit(RefView w, unsigned* data, RefFrame f, int edit_mode, uint4* __restrict__ out) {
+    float dir[3];
+    RefHit h;
+    ray_ref(w, f, 0.0f, 0.0f, 64, dir, h);
+    if (out) {
+        out[0] = make_uint4(h.data, __float_as_uint(h.hit_pos[0]), __float_as_uint(h.hit_pos[1]), __float_as_uint(h.hit_pos[2]));
+        out[1] = make_uint4(__float_as_uint(h.normal[0]), __float_as_uint(h.normal[1]), __float_as_uint(h.normal[2]), 0u);
+    }
+    if (edit_mode < 0 || h.data == 0u) return;
+    int p[3];
+    unsigned voxel;
+    if (edit_mode > 0) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) p[i] = (int)(h.hit_pos[i] + h.normal[i]) >> 3;
+        voxel = (1u << 28) + (unsigned)edit_mode - 1u;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) p[i] = (int)h.hit_pos[i] >> 3;
+        voxel = 0u;
+    }
+    const unsigned blk = ref_chunk_flags(w, p[0] >> 3, p[1] >> 3, p[2] >> 3);
+    if (blk == 0u) return;
+    const unsigned long long idx =
+        (unsigned long long)(blk - 1u) * 512ull + (unsigned long long)((p[0] % 8) + ((p[2] % 8) * 8 + (p[1] % 8)) * 8);
+    if (idx < w.ndata) data[idx] = voxel;
 }
 
 __global__ void __launch_bounds__(kRefBlock) k_render_reference(RefView w, RefFrame f, uint4* __restrict__ out) {
@@ -452,6 +491,32 @@ vt_status vt_trace_map(vt_ctx* ctx, const vt_brickmap* bm, const float* d_origin
     if (n == 0) return VT_OK;
     k_trace_map<<<(n + kRefBlock - 1) / kRefBlock, kRefBlock, 0, (cudaStream_t)stream>>>(
         view_of(bm), d_origins, d_dirs, n, max_steps, reinterpret_cast<uint4*>(d_out));
+    VT_CUDA(ctx, cudaGetLastError());
+    return VT_OK;
+}
+
+vt_status vt_brickmap_download(vt_brickmap* bm, uint32_t* h_chunks, uint32_t* h_bricks, size_t nbricks) {
+    if (!bm) return VT_ERR_ARG;
+    if (!h_chunks || (nbricks && !h_bricks) || nbricks > bm->nbricks)
+        return fail(bm->ctx, VT_ERR_ARG, "null output or more bricks than uploaded");
+    VT_CUDA(bm->ctx, cudaDeviceSynchronize());
+    VT_CUDA(bm->ctx, cudaMemcpy(h_chunks, bm->d_chunks, 64u * 64u * 64u * 4u, cudaMemcpyDeviceToHost));
+    if (nbricks) VT_CUDA(bm->ctx, cudaMemcpy(h_bricks, bm->d_data, nbricks * 512u * 4u, cudaMemcpyDeviceToHost));
+    return VT_OK;
+}
+
+vt_status vt_brickmap_edit(vt_ctx* ctx, vt_brickmap* bm, const vt_camera* cam, int32_t edit_mode, vt_ref_hit* d_out,
+                           vt_stream stream) {
+    if (!ctx) return VT_ERR_ARG;
+    if (!bm || !cam) return fail(ctx, VT_ERR_ARG, "null brickmap or camera");
+    if (edit_mode < -1 || edit_mode > (1 << 28)) return fail(ctx, VT_ERR_ARG, "edit_mode must be in [-1, 2^28]");
+    RefFrame f;
+    for (int i = 0; i < 4; ++i) f.pos[i] = cam->pos[i];
+    std::memcpy(f.view, cam->view, sizeof(f.view));
+    f.tan_half = 1.0f;  // the pick ray has UV 0 and no fov factor (terrain_edit.comp.glsl:12-14)
+    f.width = 1;
+    f.height = 1;
+    k_brickmap_edit<<<1, 1, 0, (cudaStream_t)stream>>>(view_of(bm), bm->d_data, f, edit_mode, reinterpret_cast<uint4*>(d_out));
     VT_CUDA(ctx, cudaGetLastError());
     return VT_OK;
 }

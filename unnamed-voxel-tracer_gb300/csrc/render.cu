@@ -300,8 +300,8 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
     const size_t smem = (stats || checked) ? (size_t)w.ncoarse * sizeof(unsigned long long)
                                            : (size_t)((w.nchunks + 15u) / 16u) * 16u;
     const bool use_smem = smem <= kMaxSharedCoarse;
-    if (world->dist_dirty) {
-        vt_status s = rebuild_distances(const_cast<vt_world*>(world), stream);
+    {
+        vt_status s = update_distances(const_cast<vt_world*>(world), stream);
         if (s) return s;
     }
     const size_t sm = use_smem ? smem : 0;
@@ -430,8 +430,8 @@ vt_status vt_trace_rays(vt_ctx* ctx, const vt_world* world, const float* d_origi
     if (!ctx) return VT_ERR_ARG;
     if (!world || !d_origins || !d_dirs || !d_out || n < 0) return fail(ctx, VT_ERR_ARG, "bad trace_rays arguments");
     if (n == 0) return VT_OK;
-    if (world->dist_dirty) {
-        vt_status s = rebuild_distances(const_cast<vt_world*>(world), (cudaStream_t)stream);
+    {
+        vt_status s = update_distances(const_cast<vt_world*>(world), (cudaStream_t)stream);
         if (s) return s;
     }
     const WorldView w = world->view();

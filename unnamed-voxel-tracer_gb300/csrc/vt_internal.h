@@ -81,8 +81,13 @@ struct vt_world {
     unsigned* d_palette = nullptr;
     unsigned char* d_bdist = nullptr;
     unsigned char* d_cdist = nullptr;
-    unsigned char* d_dtmp = nullptr;   // two brick-sized buffers for the distance passes
+    unsigned char* d_dtmp = nullptr;   // x and y pass results of the brick distances (kept)
+    unsigned char* d_ctmp = nullptr;   // two chunk-sized buffers for the chunk distance passes
+    int* d_edit = nullptr;             // {x, y, z, valid} of the last device-side edit
     bool dist_dirty = true;            // distances rebuilt before the next render
+    bool dist_box = false;             // bricks in [box_lo, box_hi] edited since the last update
+    int box_lo[3] = {0, 0, 0};
+    int box_hi[3] = {0, 0, 0};
     unsigned char* d_stage = nullptr;  // upload staging (grown on demand)
     size_t stage_bytes = 0;
 
@@ -114,6 +119,12 @@ vt_status check_cuda(vt_ctx* ctx, cudaError_t err, const char* what);
 vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out);
 // Rebuilds the empty-space distances of a world on `st`.
 vt_status rebuild_distances(vt_world* w, cudaStream_t st);
+// Brings the distances up to date: a full rebuild when stale, else the
+// neighbourhood of the bricks edited since the last update.
+vt_status update_distances(vt_world* w, cudaStream_t st);
+// update_distances, then the neighbourhood of the voxel {x, y, z, valid}
+// that a kernel earlier on `st` wrote to d_cell (nothing when !valid).
+vt_status update_distances_at(vt_world* w, const int* d_cell, cudaStream_t st);
 // The world's staging buffer, grown to at least `bytes` (synchronises the
 // device when it has to grow).
 vt_status world_stage(vt_world* w, size_t bytes, unsigned char** out);

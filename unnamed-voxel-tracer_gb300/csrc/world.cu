@@ -97,14 +97,25 @@ __device__ __forceinline__ unsigned brick_index(int bx, int by, int bz, int CX, 
 }
 
 // level 0: bricks (grid = 8 * chunk counts), level 1: chunks.  pass 0 reads
-// occupancy from the mask words / coarse bits, later passes read `in`.
+// occupancy from the mask words / coarse bits, later passes read `in`.  The
+// pass covers the box [lo, lo + ext) of the grid (clipped to it); when
+// `d_cell` is given, {x, y, z, valid} of an edited voxel in device memory,
+// the box is taken relative to that voxel's brick and skipped when !valid.
 __global__ void k_dist_pass(const unsigned long long* __restrict__ mask, const unsigned long long* __restrict__ coarse,
                             const unsigned char* __restrict__ in, unsigned char* __restrict__ out, int level, int axis,
-                            int CX, int CY, int CZ) {
+                            int CX, int CY, int CZ, int3 lo, int3 ext, const int* __restrict__ d_cell) {
     const int gx = level == 0 ? CX * 8 : CX, gy = level == 0 ? CY * 8 : CY, gz = level == 0 ? CZ * 8 : CZ;
-    const size_t total = (size_t)gx * gy * gz;
+    if (d_cell) {
+        if (!d_cell[3]) return;
+        lo.x += d_cell[0] >> 2;
+        lo.y += d_cell[1] >> 2;
+        lo.z += d_cell[2] >> 2;
+    }
+    const size_t total = (size_t)ext.x * ext.y * ext.z;
     for (size_t lin = blockIdx.x * (size_t)blockDim.x + threadIdx.x; lin < total; lin += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(lin % gx), y = (int)((lin / gx) % gy), z = (int)(lin / ((size_t)gx * gy));
+        const int x = lo.x + (int)(lin % ext.x), y = lo.y + (int)((lin / ext.x) % ext.y),
+                  z = lo.z + (int)(lin / ((size_t)ext.x * ext.y));
+        if (x < 0 || y < 0 || z < 0 || x >= gx || y >= gy || z >= gz) continue;
         const int g[3] = {gx, gy, gz};
         int p[3] = {x, y, z};
         const int u = p[axis];
@@ -133,24 +144,106 @@ __global__ void k_dist_pass(const unsigned long long* __restrict__ mask, const u
     }
 }
 
-vt_status rebuild_distances(vt_world* w, cudaStream_t st) {
+namespace {
+
+constexpr int kDistThreads = 256;
+
+unsigned dist_blocks(size_t n) {
+    return (unsigned)std::min<size_t>((n + kDistThreads - 1) / kDistThreads, 65535u * 4u);
+}
+
+// The three chunk-level passes over the whole chunk grid (at most a few tens
+// of thousands of cells: cheap enough to redo after any edit).
+void chunk_passes(vt_world* w, cudaStream_t st) {
     const int CX = w->cdim[0], CY = w->cdim[1], CZ = w->cdim[2];
-    const size_t nb = w->nchunks * kBricksPerChunk;
-    unsigned char* a = w->d_dtmp;
-    unsigned char* b = w->d_dtmp + nb;
-    const int threads = 256;
-    auto blocks = [&](size_t n) { return (unsigned)std::min<size_t>((n + threads - 1) / threads, 65535u * 4u); };
-    // bricks: x -> a, y -> b, z -> bdist
-    k_dist_pass<<<blocks(nb), threads, 0, st>>>(w->d_mask, w->d_coarse, nullptr, a, 0, 0, CX, CY, CZ);
-    k_dist_pass<<<blocks(nb), threads, 0, st>>>(w->d_mask, w->d_coarse, a, b, 0, 1, CX, CY, CZ);
-    k_dist_pass<<<blocks(nb), threads, 0, st>>>(w->d_mask, w->d_coarse, b, w->d_bdist, 0, 2, CX, CY, CZ);
-    // chunks
-    k_dist_pass<<<blocks(w->nchunks), threads, 0, st>>>(w->d_mask, w->d_coarse, nullptr, a, 1, 0, CX, CY, CZ);
-    k_dist_pass<<<blocks(w->nchunks), threads, 0, st>>>(w->d_mask, w->d_coarse, a, b, 1, 1, CX, CY, CZ);
-    k_dist_pass<<<blocks(w->nchunks), threads, 0, st>>>(w->d_mask, w->d_coarse, b, w->d_cdist, 1, 2, CX, CY, CZ);
+    unsigned char* a = w->d_ctmp;
+    unsigned char* b = w->d_ctmp + w->nchunks;
+    const int3 o = make_int3(0, 0, 0), g = make_int3(CX, CY, CZ);
+    k_dist_pass<<<dist_blocks(w->nchunks), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, nullptr, a, 1, 0, CX, CY, CZ, o, g, nullptr);
+    k_dist_pass<<<dist_blocks(w->nchunks), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, a, b, 1, 1, CX, CY, CZ, o, g, nullptr);
+    k_dist_pass<<<dist_blocks(w->nchunks), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, b, w->d_cdist, 1, 2, CX, CY, CZ, o, g, nullptr);
+}
+
+size_t volume(int3 e) { return (size_t)e.x * e.y * e.z; }
+
+// The brick passes: x into d_dtmp, y into d_dtmp + nbricks, z into d_bdist,
+// each over its own box.  The intermediates stay valid between calls, which
+// is what lets an edit recompute only the boxes it can change.
+void brick_passes(vt_world* w, cudaStream_t st, const int3 lo[3], const int3 ext[3], const int* d_cell) {
+    const int CX = w->cdim[0], CY = w->cdim[1], CZ = w->cdim[2];
+    unsigned char* bx = w->d_dtmp;
+    unsigned char* by = w->d_dtmp + w->nchunks * kBricksPerChunk;
+    k_dist_pass<<<dist_blocks(volume(ext[0])), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, nullptr, bx, 0, 0, CX, CY, CZ, lo[0], ext[0], d_cell);
+    k_dist_pass<<<dist_blocks(volume(ext[1])), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, bx, by, 0, 1, CX, CY, CZ, lo[1], ext[1], d_cell);
+    k_dist_pass<<<dist_blocks(volume(ext[2])), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, by, w->d_bdist, 0, 2, CX, CY, CZ, lo[2], ext[2], d_cell);
+}
+
+// After the bricks of box [blo, blo + bext) changed occupancy only these
+// cells can change: the x pass in the box +- (R, 0, 0), the y pass in the box
+// +- (R, RY, 0), the z pass in the box +- (R, RY, R), with R = kDistCap and
+// RY = kDistCap / kFlatY (a y offset beyond RY weighs more than the cap).
+// Recomputing exactly those boxes, in pass order, from the current masks
+// leaves every buffer equal to a full rebuild.
+void edit_boxes(int3 blo, int3 bext, int3 lo[3], int3 ext[3]) {
+    const int R = kDistCap, RY = kDistCap / kFlatY;
+    lo[0] = make_int3(blo.x - R, blo.y, blo.z);
+    ext[0] = make_int3(bext.x + 2 * R, bext.y, bext.z);
+    lo[1] = make_int3(blo.x - R, blo.y - RY, blo.z);
+    ext[1] = make_int3(bext.x + 2 * R, bext.y + 2 * RY, bext.z);
+    lo[2] = make_int3(blo.x - R, blo.y - RY, blo.z - R);
+    ext[2] = make_int3(bext.x + 2 * R, bext.y + 2 * RY, bext.z + 2 * R);
+}
+
+}  // namespace
+
+vt_status rebuild_distances(vt_world* w, cudaStream_t st) {
+    const int3 o = make_int3(0, 0, 0), g = make_int3(w->cdim[0] * 8, w->cdim[1] * 8, w->cdim[2] * 8);
+    const int3 lo[3] = {o, o, o}, ext[3] = {g, g, g};
+    brick_passes(w, st, lo, ext, nullptr);
+    chunk_passes(w, st);
     VT_CUDA(w->ctx, cudaGetLastError());
     w->dist_dirty = false;
+    w->dist_box = false;
     return VT_OK;
+}
+
+vt_status update_distances(vt_world* w, cudaStream_t st) {
+    if (w->dist_dirty) return rebuild_distances(w, st);
+    if (!w->dist_box) return VT_OK;
+    const int3 blo = make_int3(w->box_lo[0], w->box_lo[1], w->box_lo[2]);
+    const int3 bext = make_int3(w->box_hi[0] - w->box_lo[0] + 1, w->box_hi[1] - w->box_lo[1] + 1,
+                                w->box_hi[2] - w->box_lo[2] + 1);
+    int3 lo[3], ext[3];
+    edit_boxes(blo, bext, lo, ext);
+    if (volume(ext[2]) >= w->nchunks * kBricksPerChunk / 2) return rebuild_distances(w, st);
+    brick_passes(w, st, lo, ext, nullptr);
+    chunk_passes(w, st);
+    VT_CUDA(w->ctx, cudaGetLastError());
+    w->dist_box = false;
+    return VT_OK;
+}
+
+vt_status update_distances_at(vt_world* w, const int* d_cell, cudaStream_t st) {
+    vt_status s = update_distances(w, st);
+    if (s || w->dist_dirty) return s;
+    int3 lo[3], ext[3];
+    edit_boxes(make_int3(0, 0, 0), make_int3(1, 1, 1), lo, ext);
+    brick_passes(w, st, lo, ext, d_cell);
+    chunk_passes(w, st);
+    VT_CUDA(w->ctx, cudaGetLastError());
+    return VT_OK;
+}
+
+// Records an edit of the bricks in [lo, hi] (inclusive brick coordinates):
+// the distances near them are recomputed before the next use (unless a full
+// rebuild is pending anyway).
+static void note_edit(vt_world* w, const int lo[3], const int hi[3]) {
+    if (w->dist_dirty) return;
+    for (int i = 0; i < 3; ++i) {
+        if (!w->dist_box || lo[i] < w->box_lo[i]) w->box_lo[i] = lo[i];
+        if (!w->dist_box || hi[i] > w->box_hi[i]) w->box_hi[i] = hi[i];
+    }
+    w->dist_box = true;
 }
 
 vt_status world_stage(vt_world* w, size_t bytes, unsigned char** out) {
@@ -179,6 +272,8 @@ static void free_world(vt_world* w) {
     if (w->d_bdist) cudaFree(w->d_bdist);
     if (w->d_cdist) cudaFree(w->d_cdist);
     if (w->d_dtmp) cudaFree(w->d_dtmp);
+    if (w->d_ctmp) cudaFree(w->d_ctmp);
+    if (w->d_edit) cudaFree(w->d_edit);
     delete w;
 }
 
@@ -215,6 +310,9 @@ vt_status vt_world_create(vt_ctx* ctx, const vt_world_desc* desc, vt_world** out
         (e = cudaMalloc(&w->d_bdist, w->nchunks * kBricksPerChunk)) != cudaSuccess ||
         (e = cudaMalloc(&w->d_cdist, (w->nchunks + 15) / 16 * 16)) != cudaSuccess ||
         (e = cudaMalloc(&w->d_dtmp, 2 * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_ctmp, 2 * w->nchunks)) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_edit, 4 * sizeof(int))) != cudaSuccess ||
+        (e = cudaMemset(w->d_edit, 0, 4 * sizeof(int))) != cudaSuccess ||
         (e = cudaMemset(w->d_mask, 0, w->nchunks * kBricksPerChunk * 8)) != cudaSuccess ||
         (e = cudaMemset(w->d_mats, 0, w->nchunks * (size_t)kChunkBytes)) != cudaSuccess ||
         (e = cudaMemset(w->d_coarse, 0, w->ncoarse * 8)) != cudaSuccess) {
@@ -282,7 +380,8 @@ vt_status vt_world_upload_chunk(vt_world* w, int32_t cx, int32_t cy, int32_t cz,
     k_build_chunks<<<1, 512, 0, st>>>(w->view(), w->d_mask, w->d_mats, w->d_coarse, w->d_stage, make_int3(32, 32, 32),
                                       make_int3(cx * 32, cy * 32, cz * 32), make_int3(cx, cy, cz), make_int3(1, 1, 1));
     VT_CUDA(w->ctx, cudaGetLastError());
-    w->dist_dirty = true;
+    const int blo[3] = {cx * 8, cy * 8, cz * 8}, bhi[3] = {cx * 8 + 7, cy * 8 + 7, cz * 8 + 7};
+    note_edit(w, blo, bhi);
     VT_CUDA(w->ctx, cudaStreamSynchronize(st));
     return VT_OK;
 }
@@ -293,7 +392,8 @@ vt_status vt_world_set_voxel(vt_world* w, int32_t x, int32_t y, int32_t z, uint8
         return fail(w->ctx, VT_ERR_ARG, "voxel coordinate out of range");
     k_set_voxel<<<1, 512, 0, (cudaStream_t)stream>>>(w->view(), w->d_mask, w->d_mats, w->d_coarse, x, y, z, material);
     VT_CUDA(w->ctx, cudaGetLastError());
-    w->dist_dirty = true;
+    const int b[3] = {x >> 2, y >> 2, z >> 2};
+    note_edit(w, b, b);
     return VT_OK;
 }
 

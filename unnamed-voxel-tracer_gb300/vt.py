@@ -143,6 +143,11 @@ _SIGNATURES = {
     "vt_vox_decode": (_S, [_P, C.c_size_t, _P, C.c_int32, C.POINTER(C.c_int32)]),
     "vt_trace_map": (_S, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, _P]),
     "vt_render_reference": (_S, [_P, _P, C.POINTER(Camera_t), _P, _P]),
+    "vt_brickmap_edit": (_S, [_P, _P, C.POINTER(Camera_t), C.c_int32, _P, _P]),
+    "vt_brickmap_download": (_S, [_P, _P, _P, C.c_size_t]),
+    "vt_pick": (_S, [_P, _P, C.POINTER(Camera_t), C.c_int32, _P]),
+    "vt_edit": (_S, [_P, _P, C.POINTER(Camera_t), C.c_int32, C.c_int32, _P, _P]),
+    "vt_world_download_distances": (_S, [_P, _P, C.c_size_t, _P, C.c_size_t]),
     "vt_batch_create": (_S, [_P, C.POINTER(Job_t), C.c_int32, C.POINTER(Params_t), C.POINTER(_P)]),
     "vt_batch_launch": (_S, [_P, _P]),
     "vt_batch_destroy": (_S, [_P]),
@@ -342,6 +347,25 @@ class World:
     def clear(self, stream=None) -> None:
         self.ctx.check(self.ctx.lib.vt_world_clear(self.handle, stream))
 
+    def pick(self, cam: Camera_t, max_steps: int) -> np.ndarray:
+        """The centre-of-view pick ray's hit record (vt_pick)."""
+        out = np.zeros(1, dtype=HIT_DTYPE)
+        self.ctx.check(self.ctx.lib.vt_pick(self.ctx.handle, self.handle, C.byref(cam), int(max_steps), _ptr(out)))
+        return out[0]
+
+    def edit(self, cam: Camera_t, max_steps: int, edit_mode: int, d_out=None, stream=None) -> None:
+        """Pick and edit on the device (vt_edit); d_out: optional DeviceBuffer."""
+        self.ctx.check(self.ctx.lib.vt_edit(self.ctx.handle, self.handle, C.byref(cam), int(max_steps), int(edit_mode),
+                                            d_out.ptr if d_out is not None else None, stream))
+
+    def distances(self):
+        """(brick distances [nchunks*512], chunk distances [nchunks]) as uint8."""
+        i = self.info()
+        nch = i.chunks[0] * i.chunks[1] * i.chunks[2]
+        b, c = np.zeros(nch * 512, np.uint8), np.zeros(nch, np.uint8)
+        self.ctx.check(self.ctx.lib.vt_world_download_distances(self.handle, _ptr(b), b.nbytes, _ptr(c), c.nbytes))
+        return b, c
+
     def set_palette(self, rgba: np.ndarray) -> None:
         rgba = np.ascontiguousarray(rgba, dtype=np.uint32)
         assert rgba.size == 256
@@ -482,6 +506,23 @@ class Brickmap:
             return d.download(np.zeros(n, REF_PIXEL_DTYPE))
         finally:
             d.free()
+
+    def edit(self, cam: Camera_t, edit_mode: int) -> np.ndarray:
+        """The editing pass (pick + map_setVoxel); returns the pick's hit."""
+        ctx = self.ctx
+        d = ctx.alloc(32)
+        try:
+            ctx.check(ctx.lib.vt_brickmap_edit(ctx.handle, self.handle, C.byref(cam), int(edit_mode), d.ptr, None))
+            ctx.sync()
+            return d.download(np.zeros(1, REF_HIT_DTYPE))[0]
+        finally:
+            d.free()
+
+    def download(self, nbricks: int):
+        """(chunk table [64^3], first nbricks bricks [nbricks*512]) as uint32."""
+        ch, br = np.zeros(64 ** 3, np.uint32), np.zeros(nbricks * 512, np.uint32)
+        self.ctx.check(self.ctx.lib.vt_brickmap_download(self.handle, _ptr(ch), _ptr(br), nbricks))
+        return ch, br
 
     def close(self) -> None:
         if self.handle:
