@@ -188,6 +188,18 @@ def run_reference(args, rank: int, world: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+def aggregate(torch, dist, world: int, device, rays: float, ms: float, e2e_s: float) -> tuple[float, float, float]:
+    """Whole-job totals of a replica run: rays summed over ranks, device and
+    end-to-end times maxed over ranks (the job ends with its slowest rank)."""
+    if world == 1:
+        return rays, ms, e2e_s
+    r = torch.tensor([rays], dtype=torch.float64, device=device)
+    t = torch.tensor([ms, e2e_s], dtype=torch.float64, device=device)
+    dist.all_reduce(r, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(r[0]), float(t[0]), float(t[1])
+
+
 def _timed(torch, fn, reps: int) -> float:
     """Mean ms of fn() over reps runs, CUDA events on the current stream."""
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -387,12 +399,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             e2e_s += time.perf_counter() - t0
     ctx.lib.vt_host_free_pinned(ctx.handle, hbuf)
 
-    t = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms, e2e_s = float(t[0]), float(t[1])
-    value = world * total_rays / (total_ms * 1e-3) / 1e9
-    e2e_value = world * total_rays / e2e_s / 1e9
+    job_rays, total_ms, e2e_s = aggregate(torch, dist, world, dev, total_rays, total_ms, e2e_s)
+    value = job_rays / (total_ms * 1e-3) / 1e9
+    e2e_value = job_rays / e2e_s / 1e9
 
     if rank != 0:
         return
@@ -431,7 +440,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                      "algorithmic_bytes_per_step": total_bytes / args.steps, "traffic_note": traffic_note},
         "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2,
                         "peak_kind": "24 MiB device copy held in L2, read+write bytes, this run"},
-        "rays_per_step": total_rays / args.steps,
+        "rays_per_step": job_rays / args.steps,
         "per_ray": {k: sum(s[k] for s in stats) / sum(rays) for k in ("steps", "iterations", "mask_words",
                                                                        "coarse_words")},
         "e2e": {"value": e2e_value, "unit": "Grays/s", "h2d_bytes_per_step": C.sizeof(vt.Camera_t) + C.sizeof(vt.Params_t),
