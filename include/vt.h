@@ -125,6 +125,14 @@ vt_status vt_world_download_dense(vt_world* world, uint8_t* h_materials, size_t 
  * REFERENCE shading mode (the role of the model atlas texel, map.glsl:57-60). */
 vt_status vt_world_set_palette(vt_world* world, const uint32_t* h_rgba256);
 vt_status vt_world_get_info(const vt_world* world, vt_world_info* info);
+/* Entity occluders of the shadow pass (traceEntities, map.glsl:172-201, as
+ * used by secondary.comp.glsl:42-46, which tests five hard-coded unit boxes):
+ * n <= 1024 axis-aligned boxes {lo x, y, z, hi x, y, z} in voxel units.  A
+ * shadow ray clear of voxels that meets a box (t >= 0) shades its pixel as
+ * shadowed and sets VT_HIT_ENTITY.  Synchronous; takes effect for work queued
+ * afterwards (do not call while a render of this world is in flight).  n = 0
+ * removes them. */
+vt_status vt_world_set_entities(vt_world* world, const float* h_boxes, int32_t n);
 
 /* ------------------------------------------------------------------ camera
  * Mirrors Camera.UniformData (camera.zig:12-16, camera.glsl:2-6) plus the
@@ -187,6 +195,7 @@ typedef struct {
 #define VT_HIT_PRIMARY   1u /* primary ray hit a voxel */
 #define VT_HIT_SHADOWED  2u /* shadow ray hit a voxel */
 #define VT_HIT_BOUNCE    4u /* bounce ray hit a voxel */
+#define VT_HIT_ENTITY    8u /* shadow ray clear of voxels but met an entity box: shaded as shadowed */
 
 void vt_params_default(vt_params* p);
 

@@ -24,7 +24,8 @@ _spec.loader.exec_module(_build)
 
 
 class VtoWorld_t(C.Structure):
-    _fields_ = [("dims", C.c_int32 * 3), ("mats", C.c_void_p), ("chunk_occ", C.c_void_p), ("chunks", C.c_int32 * 3)]
+    _fields_ = [("dims", C.c_int32 * 3), ("mats", C.c_void_p), ("chunk_occ", C.c_void_p), ("chunks", C.c_int32 * 3),
+                ("entities", C.c_void_p), ("n_entities", C.c_int32)]
 
 
 class VtoTrace_t(C.Structure):
@@ -91,7 +92,7 @@ def load() -> C.CDLL:
 class OracleWorld:
     """A dense mode-P world (uint8 array [z, y, x]) seen by the oracle."""
 
-    def __init__(self, mats: np.ndarray):
+    def __init__(self, mats: np.ndarray, entities: np.ndarray | None = None):
         self.mats = np.ascontiguousarray(mats, dtype=np.uint8)
         Z, Y, X = self.mats.shape
         self.dims = (X, Y, Z)
@@ -99,6 +100,10 @@ class OracleWorld:
         dims = (C.c_int32 * 3)(X, Y, Z)
         if load().vto_world_init(C.byref(self.w), dims, self.mats.ctypes.data) != 0:
             raise MemoryError("oracle world init failed")
+        if entities is not None:
+            self.entities = np.ascontiguousarray(entities, dtype=np.float32).reshape(-1, 6)
+            self.w.entities = self.entities.ctypes.data
+            self.w.n_entities = self.entities.shape[0]
 
     def __del__(self):
         if _lib is not None and getattr(self, "w", None) is not None:

@@ -267,6 +267,30 @@ static void primary_ray(const vt_camera* cam, int px, int py, float o[3], float 
     }
 }
 
+/* Entity occluders (traceEntities' role in secondary.comp.glsl:42-46, as a
+ * list of boxes): the ray o + t d, t >= 0, against the closed box {lo, hi};
+ * slab test with IEEE division, an axis without motion must lie in its slab. */
+static int ray_box(const float o[3], const float d[3], const float* box) {
+    float tmin = 0.0f, tmax = INFINITY;
+    for (int j = 0; j < 3; ++j) {
+        if (d[j] == 0.0f) {
+            if (o[j] < box[j] || o[j] > box[3 + j]) return 0;
+            continue;
+        }
+        const float a = (box[j] - o[j]) / d[j], b = (box[3 + j] - o[j]) / d[j];
+        const float lo = a < b ? a : b, hi = a < b ? b : a;
+        if (lo > tmin) tmin = lo;
+        if (hi < tmax) tmax = hi;
+    }
+    return tmin <= tmax;
+}
+
+static int entity_occluded(const vto_world* w, const float o[3], const float d[3]) {
+    for (int i = 0; i < w->n_entities; ++i)
+        if (ray_box(o, d, w->entities + 6 * i)) return 1;
+    return 0;
+}
+
 static float clampf(float x, float a, float b) { return x < a ? a : (x > b ? b : x); }
 
 static uint32_t unorm8(float x) { return (uint32_t)(int)rintf(clampf(x, 0.0f, 1.0f) * 255.0f); }
@@ -391,6 +415,9 @@ static void shade_pixel(const vto_world* w, const uint32_t* palette, const vt_ca
                 shadowed = 1;
                 h.flags |= VT_HIT_SHADOWED;
                 if (st) st->shadow_hits++;
+            } else if (entity_occluded(w, so, p->sun_dir)) {
+                shadowed = 1;
+                h.flags |= VT_HIT_ENTITY;
             }
         }
         int bounce_open = 0;
@@ -587,7 +614,7 @@ int32_t vto_shade_grad_f64(const vto_world* w, const vt_camera* cam, const vt_hi
                 } else {
                     vto_trace ts;
                     vto_trace_p(w, so, sunf, shadow_max_steps, &ts);
-                    lit = !ts.hit;
+                    lit = !ts.hit && !entity_occluded(w, so, sunf);
                 }
                 ndl = nrm[0] * sn[0] + nrm[1] * sn[1] + nrm[2] * sn[2];
                 shade = ka + kd * (ndl > 0.0 ? ndl : 0.0) * (lit ? 1.0 : 0.0);

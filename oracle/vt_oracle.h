@@ -40,6 +40,10 @@ typedef struct {
     /* derived, owned by the oracle (vto_world_init / vto_world_free) */
     uint8_t* chunk_occ;   /* per 32^3 chunk */
     int32_t chunks[3];
+    /* entity occluders of the shadow pass (vt_world_set_entities): n boxes
+     * {lo x, y, z, hi x, y, z}; set by the caller after vto_world_init */
+    const float* entities;
+    int32_t n_entities;
 } vto_world;
 
 int32_t vto_world_init(vto_world* w, const int32_t dims[3], const uint8_t* mats);

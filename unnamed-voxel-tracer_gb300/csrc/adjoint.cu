@@ -119,7 +119,8 @@ __global__ void __launch_bounds__(kAdjBlock) k_shade(AdjArgs a) {
                 PRay rs;
                 pray_init(rs, so, a.sun);
                 TraceHit hs;
-                lit = !trace_fast<false>(a.w, cd, rs, a.shadow_steps, hs);
+                lit = !trace_fast<false>(a.w, cd, rs, a.shadow_steps, hs) &&
+                      !(a.w.n_entities > 0 && entity_occluded(a.w, so, a.sun));
             }
             ndl_raw = dot3(nrm, a.sun_n);
             const float ndl = ndl_raw > 0.0f ? ndl_raw : 0.0f;

@@ -72,6 +72,10 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
                 pc.v[2] += 1;
                 pc.v[3] += shadowed ? 1u : 0u;
             }
+            if (!shadowed && w.n_entities > 0 && entity_occluded(w, so, f.sun)) {
+                shadowed = true;
+                flags |= VT_HIT_ENTITY;
+            }
         }
         bool bounce_open = false;
         float bdir[3] = {0.0f, 0.0f, 0.0f};

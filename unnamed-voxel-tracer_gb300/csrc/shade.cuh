@@ -50,6 +50,32 @@ __device__ __forceinline__ void primary_ray(const FrameParams& f, int px, int py
     }
 }
 
+// Entity occluders (the role of traceEntities, map.glsl:172-201, in the
+// shadow pass, secondary.comp.glsl:42-46): true when the ray o + t d, t >= 0,
+// meets the closed box {lo[3], hi[3]}.  Slab test with IEEE division; an axis
+// the ray does not move along is inside its slab or misses.
+__host__ __device__ __forceinline__ bool ray_box(const float o[3], const float d[3], const float* box) {
+    float tmin = 0.0f, tmax = INFINITY;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        if (d[j] == 0.0f) {
+            if (o[j] < box[j] || o[j] > box[3 + j]) return false;
+            continue;
+        }
+        const float a = (box[j] - o[j]) / d[j], b = (box[3 + j] - o[j]) / d[j];
+        const float lo = a < b ? a : b, hi = a < b ? b : a;
+        tmin = lo > tmin ? lo : tmin;
+        tmax = hi < tmax ? hi : tmax;
+    }
+    return tmin <= tmax;
+}
+
+__device__ __forceinline__ bool entity_occluded(const WorldView& w, const float o[3], const float d[3]) {
+    for (int i = 0; i < w.n_entities; ++i)
+        if (ray_box(o, d, w.entities + 6 * i)) return true;
+    return false;
+}
+
 // Shared by host and device: plain IEEE operators (correctly rounded division
 // and square root on both sides, no contraction).
 __host__ __device__ __forceinline__ float clampf(float x, float a, float b) { return x < a ? a : (x > b ? b : x); }

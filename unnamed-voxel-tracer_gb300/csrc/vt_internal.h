@@ -31,6 +31,8 @@ struct WorldView {
     const unsigned char* bdist;         // per brick: 0 if occupied, else Chebyshev distance in bricks
                                         // to the nearest occupied brick, capped at kDistCap + 1
     const unsigned char* cdist;         // per chunk: same, in chunks
+    const float* entities;              // n_entities boxes {lo x, y, z, hi x, y, z}: shadow occluders
+    int n_entities;
     int dims[3];
     int cdim[3];                        // chunk counts
     unsigned nwords;                    // number of brick words
@@ -46,6 +48,8 @@ constexpr int kDistCap = 15;
 // (radius d-1 across, (d-1)/kFlatY up and down), which suits rays that skim
 // terrain; the chunk distance is plain Chebyshev.
 constexpr int kFlatY = 4;
+// Capacity of a world's entity box list.
+constexpr int kMaxEntities = 1024;
 
 }  // namespace vt
 
@@ -84,6 +88,8 @@ struct vt_world {
     unsigned char* d_dtmp = nullptr;   // x and y pass results of the brick distances (kept)
     unsigned char* d_ctmp = nullptr;   // two chunk-sized buffers for the chunk distance passes
     int* d_edit = nullptr;             // {x, y, z, valid} of the last device-side edit
+    float* d_entities = nullptr;       // kMaxEntities boxes of 6 floats
+    int n_entities = 0;
     bool dist_dirty = true;            // distances rebuilt before the next render
     bool dist_box = false;             // bricks in [box_lo, box_hi] edited since the last update
     int box_lo[3] = {0, 0, 0};
@@ -99,6 +105,8 @@ struct vt_world {
         v.palette = d_palette;
         v.bdist = d_bdist;
         v.cdist = d_cdist;
+        v.entities = d_entities;
+        v.n_entities = n_entities;
         v.nchunks = (unsigned)nchunks;
         for (int i = 0; i < 3; ++i) {
             v.dims[i] = dims[i];

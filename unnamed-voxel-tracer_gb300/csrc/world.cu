@@ -274,6 +274,7 @@ static void free_world(vt_world* w) {
     if (w->d_dtmp) cudaFree(w->d_dtmp);
     if (w->d_ctmp) cudaFree(w->d_ctmp);
     if (w->d_edit) cudaFree(w->d_edit);
+    if (w->d_entities) cudaFree(w->d_entities);
     delete w;
 }
 
@@ -312,6 +313,7 @@ vt_status vt_world_create(vt_ctx* ctx, const vt_world_desc* desc, vt_world** out
         (e = cudaMalloc(&w->d_dtmp, 2 * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
         (e = cudaMalloc(&w->d_ctmp, 2 * w->nchunks)) != cudaSuccess ||
         (e = cudaMalloc(&w->d_edit, 4 * sizeof(int))) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_entities, kMaxEntities * 6 * sizeof(float))) != cudaSuccess ||
         (e = cudaMemset(w->d_edit, 0, 4 * sizeof(int))) != cudaSuccess ||
         (e = cudaMemset(w->d_mask, 0, w->nchunks * kBricksPerChunk * 8)) != cudaSuccess ||
         (e = cudaMemset(w->d_mats, 0, w->nchunks * (size_t)kChunkBytes)) != cudaSuccess ||
@@ -413,6 +415,17 @@ vt_status vt_world_set_palette(vt_world* w, const uint32_t* h_rgba256) {
     if (!w) return VT_ERR_ARG;
     if (!h_rgba256) return fail(w->ctx, VT_ERR_ARG, "null palette");
     VT_CUDA(w->ctx, cudaMemcpy(w->d_palette, h_rgba256, 256 * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    return VT_OK;
+}
+
+vt_status vt_world_set_entities(vt_world* w, const float* h_boxes, int32_t n) {
+    if (!w) return VT_ERR_ARG;
+    if (n < 0 || n > kMaxEntities || (n > 0 && !h_boxes))
+        return fail(w->ctx, VT_ERR_ARG, "entity count must be in [0, 1024] with a box list");
+    for (int i = 0; i < 6 * n; ++i)
+        if (!(h_boxes[i] == h_boxes[i])) return fail(w->ctx, VT_ERR_ARG, "entity box coordinates must not be NaN");
+    if (n > 0) VT_CUDA(w->ctx, cudaMemcpy(w->d_entities, h_boxes, (size_t)n * 6 * sizeof(float), cudaMemcpyHostToDevice));
+    w->n_entities = n;
     return VT_OK;
 }
 

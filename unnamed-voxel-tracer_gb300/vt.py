@@ -34,7 +34,7 @@ RAYS_PRIMARY, RAYS_SHADOW, RAYS_BOUNCE = 1, 2, 4
 SHADE_NONE, SHADE_REFERENCE, SHADE_LAMBERT = 0, 1, 2
 FLAG_CROSSHAIR, FLAG_VIGNETTE, FLAG_CHECKED = 1, 2, 4
 KERNEL_TILE, KERNEL_QUEUE = 0, 1
-HIT_PRIMARY, HIT_SHADOWED, HIT_BOUNCE = 1, 2, 4
+HIT_PRIMARY, HIT_SHADOWED, HIT_BOUNCE, HIT_ENTITY = 1, 2, 4, 8
 
 
 class Camera_t(C.Structure):
@@ -123,6 +123,7 @@ _SIGNATURES = {
     "vt_world_set_voxel": (_S, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_uint8, _P]),
     "vt_world_get_voxel": (_S, [_P, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_uint8)]),
     "vt_world_download_dense": (_S, [_P, _P, C.c_size_t, _P]),
+    "vt_world_set_entities": (_S, [_P, _P, C.c_int32]),
     "vt_world_set_palette": (_S, [_P, _P]),
     "vt_world_get_info": (_S, [_P, C.POINTER(WorldInfo_t)]),
     "vt_camera_look": (_S, [C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float, C.c_int32, C.c_int32,
@@ -346,6 +347,11 @@ class World:
 
     def clear(self, stream=None) -> None:
         self.ctx.check(self.ctx.lib.vt_world_clear(self.handle, stream))
+
+    def set_entities(self, boxes) -> None:
+        """Entity occluders of the shadow pass: (n, 6) boxes {lo xyz, hi xyz}."""
+        b = np.ascontiguousarray(boxes if boxes is not None else np.zeros((0, 6)), dtype=np.float32).reshape(-1, 6)
+        self.ctx.check(self.ctx.lib.vt_world_set_entities(self.handle, _ptr(b) if b.size else None, b.shape[0]))
 
     def pick(self, cam: Camera_t, max_steps: int) -> np.ndarray:
         """The centre-of-view pick ray's hit record (vt_pick)."""
