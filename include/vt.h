@@ -410,8 +410,12 @@ vt_status vt_pick(vt_ctx* ctx, vt_world* world, const vt_camera* cam, int32_t ma
 vt_status vt_edit(vt_ctx* ctx, vt_world* world, const vt_camera* cam, int32_t max_steps, int32_t edit_mode,
                   vt_hit* d_out, vt_stream stream);
 /* The empty-space distances the traversal skips by (brought up to date
- * first): one byte per brick (chunk-major, 512 per chunk, brick bx + 8*(by +
- * 8*bz)) and one per chunk.  For tests and tools. */
+ * first), one field per direction octant o (bit i of o set: towards +i):
+ * h_brick gets 8 fields of nchunks*512 bytes (chunk-major, brick bx + 8*(by
+ * + 8*bz)), h_chunk 8 fields of nchunks bytes.  Entry d of octant o: 0 if
+ * occupied, else min over occupied cells ahead in that octant of
+ * max(|dx|, w|dy|, |dz|) (w = 4 for bricks, 1 for chunks), capped at 16.
+ * For tests and tools. */
 vt_status vt_world_download_distances(vt_world* world, uint8_t* h_brick, size_t brick_bytes, uint8_t* h_chunk,
                                       size_t chunk_bytes);
 

@@ -28,27 +28,99 @@ static inline unsigned atomicOr(unsigned* p, unsigned v) { unsigned o = *p; *p |
 #include "../../unnamed-voxel-tracer_gb300/csrc/trace_p.cuh"
 
 // Distance max(|dx|, wy*|dy|, |dz|) (capped at kDistCap + 1) from each cell of
-// a gx*gy*gz occupancy grid to the nearest occupied cell, by brute force over
-// growing shells.
-static std::vector<unsigned char> cheb(const std::vector<unsigned char>& occ, int gx, int gy, int gz, int wy) {
+// a gx*gy*gz occupancy grid to the nearest occupied cell ahead in octant oct
+// (bit i set: d_i >= 0, else d_i <= 0).  Computed independently of the
+// library's separable passes: the smallest r whose box (r cells ahead in x
+// and z, r / wy in y) holds an occupied cell, counted with a summed-area
+// table.
+static std::vector<unsigned char> cheb(const std::vector<unsigned char>& occ, int gx, int gy, int gz, int wy,
+                                       int oct) {
     const int cap = vt::kDistCap;
+    const size_t sx = gx + 1, sy = gy + 1;
+    std::vector<int> sat(sx * sy * (gz + 1), 0);
+    auto S = [&](int x, int y, int z) -> int& { return sat[(size_t)x + sx * ((size_t)y + sy * z)]; };
+    for (int z = 0; z < gz; ++z)
+        for (int y = 0; y < gy; ++y)
+            for (int x = 0; x < gx; ++x)
+                S(x + 1, y + 1, z + 1) = occ[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] + S(x, y + 1, z + 1) +
+                                         S(x + 1, y, z + 1) + S(x + 1, y + 1, z) - S(x, y, z + 1) - S(x, y + 1, z) -
+                                         S(x + 1, y, z) + S(x, y, z);
+    auto count = [&](int x0, int x1, int y0, int y1, int z0, int z1) {  // inclusive, clipped
+        x0 = std::max(x0, 0); y0 = std::max(y0, 0); z0 = std::max(z0, 0);
+        x1 = std::min(x1, gx - 1); y1 = std::min(y1, gy - 1); z1 = std::min(z1, gz - 1);
+        if (x0 > x1 || y0 > y1 || z0 > z1) return 0;
+        return S(x1 + 1, y1 + 1, z1 + 1) - S(x0, y1 + 1, z1 + 1) - S(x1 + 1, y0, z1 + 1) - S(x1 + 1, y1 + 1, z0) +
+               S(x0, y0, z1 + 1) + S(x0, y1 + 1, z0) + S(x1 + 1, y0, z0) - S(x0, y0, z0);
+    };
     std::vector<unsigned char> d((size_t)gx * gy * gz);
     for (int z = 0; z < gz; ++z)
         for (int y = 0; y < gy; ++y)
             for (int x = 0; x < gx; ++x) {
                 int best = cap + 1;
-                for (int r = 0; r <= cap && best > cap; ++r)
-                    for (int dz = -r; dz <= r && best > cap; ++dz)
-                        for (int dy = -r; dy <= r && best > cap; ++dy)
-                            for (int dx = -r; dx <= r; ++dx) {
-                                if (std::max(std::abs(dx), std::max(wy * std::abs(dy), std::abs(dz))) != r) continue;
-                                int qx = x + dx, qy = y + dy, qz = z + dz;
-                                if (qx < 0 || qy < 0 || qz < 0 || qx >= gx || qy >= gy || qz >= gz) continue;
-                                if (occ[(size_t)qx + (size_t)gx * ((size_t)qy + (size_t)gy * qz)]) { best = r; break; }
-                            }
+                for (int r = 0; r <= cap; ++r) {
+                    const int rx = r, ry = r / wy, rz = r;
+                    const int x0 = (oct & 1) ? x : x - rx, x1 = (oct & 1) ? x + rx : x;
+                    const int y0 = (oct & 2) ? y : y - ry, y1 = (oct & 2) ? y + ry : y;
+                    const int z0 = (oct & 4) ? z : z - rz, z1 = (oct & 4) ? z + rz : z;
+                    if (count(x0, x1, y0, y1, z0, z1) > 0) {
+                        best = r;
+                        break;
+                    }
+                }
                 d[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] = (unsigned char)best;
             }
     return d;
+}
+
+// The 8 octant fields of brick and chunk distances for a world's mask words,
+// in the library's layout (chunk fields `cstride` bytes apart).
+static void distances(const int cd[3], const std::vector<unsigned long long>& mask, std::vector<unsigned char>& bdist,
+                      std::vector<unsigned char>& cdist, size_t cstride) {
+    const size_t nch = (size_t)cd[0] * cd[1] * cd[2];
+    const int gx = cd[0] * 8, gy = cd[1] * 8, gz = cd[2] * 8;
+    std::vector<unsigned char> bocc((size_t)gx * gy * gz), cocc(nch);
+    for (int z = 0; z < gz; ++z)
+        for (int y = 0; y < gy; ++y)
+            for (int x = 0; x < gx; ++x) {
+                size_t ci = (size_t)(x >> 3) + cd[0] * ((size_t)(y >> 3) + (size_t)cd[1] * (z >> 3));
+                unsigned bi = (x & 7) | ((y & 7) << 3) | ((z & 7) << 6);
+                bocc[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] = mask[ci * 512 + bi] != 0;
+                if (mask[ci * 512 + bi]) cocc[ci] = 1;
+            }
+    bdist.assign(vt::kOctants * nch * 512, 0);
+    cdist.assign(vt::kOctants * cstride, 0);
+    for (int o = 0; o < vt::kOctants; ++o) {
+        std::vector<unsigned char> bd = cheb(bocc, gx, gy, gz, vt::kFlatY, o), cdd = cheb(cocc, cd[0], cd[1], cd[2], 1, o);
+        for (int z = 0; z < gz; ++z)
+            for (int y = 0; y < gy; ++y)
+                for (int x = 0; x < gx; ++x) {
+                    size_t ci = (size_t)(x >> 3) + cd[0] * ((size_t)(y >> 3) + (size_t)cd[1] * (z >> 3));
+                    unsigned bi = (x & 7) | ((y & 7) << 3) | ((z & 7) << 6);
+                    bdist[o * nch * 512 + ci * 512 + bi] = bd[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)];
+                }
+        std::copy(cdd.begin(), cdd.end(), cdist.begin() + (size_t)o * cstride);
+    }
+}
+
+// The same fields for a dense world (X*Y*Z bytes), chunk fields packed
+// (nchunks bytes apart), the layout vt_world_download_distances returns.
+extern "C" void ht_distances(const int32_t dims[3], const uint8_t* dense, uint8_t* h_brick, uint8_t* h_chunk) {
+    int cd[3];
+    for (int i = 0; i < 3; ++i) cd[i] = (dims[i] + 31) / 32;
+    const size_t nch = (size_t)cd[0] * cd[1] * cd[2];
+    std::vector<unsigned long long> mask(nch * 512, 0ull);
+    for (int z = 0; z < dims[2]; ++z)
+        for (int y = 0; y < dims[1]; ++y)
+            for (int x = 0; x < dims[0]; ++x)
+                if (dense[(size_t)x + (size_t)dims[0] * ((size_t)y + (size_t)dims[1] * z)]) {
+                    size_t ci = (size_t)(x >> 5) + cd[0] * ((size_t)(y >> 5) + (size_t)cd[1] * (z >> 5));
+                    unsigned bi = ((x >> 2) & 7) | (((y >> 2) & 7) << 3) | (((z >> 2) & 7) << 6);
+                    mask[ci * 512 + bi] |= 1ull << ((x & 3) | ((y & 3) << 2) | ((z & 3) << 4));
+                }
+    std::vector<unsigned char> b, c;
+    distances(cd, mask, b, c, nch);
+    std::copy(b.begin(), b.end(), h_brick);
+    std::copy(c.begin(), c.end(), h_chunk);
 }
 
 extern "C" int ht_trace_rays(const int32_t dims[3], const uint8_t* dense, const float* origins, const float* dirs,
@@ -82,28 +154,13 @@ extern "C" int ht_trace_rays(const int32_t dims[3], const uint8_t* dense, const 
     w.nwords = (unsigned)(nch * 512);
     w.ncoarse = (unsigned)coarse.size();
     // empty-space distances in the kernel's brick order and chunk order
-    const int gx = cd[0] * 8, gy = cd[1] * 8, gz = cd[2] * 8;
-    std::vector<unsigned char> bocc((size_t)gx * gy * gz), cocc(nch);
-    for (int z = 0; z < gz; ++z)
-        for (int y = 0; y < gy; ++y)
-            for (int x = 0; x < gx; ++x) {
-                size_t ci = (size_t)(x >> 3) + cd[0] * ((size_t)(y >> 3) + (size_t)cd[1] * (z >> 3));
-                unsigned bi = (x & 7) | ((y & 7) << 3) | ((z & 7) << 6);
-                bocc[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] = mask[ci * 512 + bi] != 0;
-                if (mask[ci * 512 + bi]) cocc[ci] = 1;
-            }
-    std::vector<unsigned char> bd = cheb(bocc, gx, gy, gz, vt::kFlatY), cdd = cheb(cocc, cd[0], cd[1], cd[2], 1);
-    std::vector<unsigned char> bdist(nch * 512);
-    for (int z = 0; z < gz; ++z)
-        for (int y = 0; y < gy; ++y)
-            for (int x = 0; x < gx; ++x) {
-                size_t ci = (size_t)(x >> 3) + cd[0] * ((size_t)(y >> 3) + (size_t)cd[1] * (z >> 3));
-                unsigned bi = (x & 7) | ((y & 7) << 3) | ((z & 7) << 6);
-                bdist[ci * 512 + bi] = bd[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)];
-            }
+    const unsigned cstride = vt::cdist_stride((unsigned)nch);
+    std::vector<unsigned char> bdist, cdist;
+    distances(cd, mask, bdist, cdist, cstride);
     w.bdist = bdist.data();
-    w.cdist = cdd.data();
+    w.cdist = cdist.data();
     w.nchunks = (unsigned)nch;
+    w.cstride = cstride;
     unsigned status = 0;
     for (int i = 0; i < n; ++i) {
         vt::PRay r;

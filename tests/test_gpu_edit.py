@@ -37,6 +37,50 @@ def assert_same_distances(vt, ctx, world, mats):
     assert bad.size == 0, (bad[:8], b[bad[:8]], fb[bad[:8]])
 
 
+@pytest.fixture(scope="module")
+def host_fields():
+    """Distance fields computed on the host by an independent method (a
+    summed-area table per octant, tests/host/trace_host.cpp)."""
+    import ctypes as C
+    import subprocess
+    import test_host_trace as T
+    if not T.OUT.exists() or any(d.stat().st_mtime > T.OUT.stat().st_mtime for d in T.DEPS):
+        T.OUT.parent.mkdir(exist_ok=True)
+        subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", T.cuda_include(),
+                        str(T.SRC), "-o", str(T.OUT)], check=True)
+    lib = C.CDLL(str(T.OUT))
+    lib.ht_distances.argtypes = [C.POINTER(C.c_int32), C.c_void_p, C.c_void_p, C.c_void_p]
+
+    def fields(mats):
+        Z, Y, X = mats.shape
+        nch = ((X + 31) // 32) * ((Y + 31) // 32) * ((Z + 31) // 32)
+        b, c = np.zeros((8, nch * 512), np.uint8), np.zeros((8, nch), np.uint8)
+        m = np.ascontiguousarray(mats)
+        lib.ht_distances((C.c_int32 * 3)(X, Y, Z), m.ctypes.data, b.ctypes.data, c.ctypes.data)
+        return b, c
+    return fields
+
+
+@pytest.mark.parametrize("dims,seed", [((70, 45, 90), 1), ((160, 96, 128), 2), ((33, 200, 40), 3)])
+def test_distances_equal_independent_computation(vt, ctx, host_fields, dims, seed):
+    desc = vt.gen_desc(dims, scale=0.5, seed=seed, trees=30, caves=True)
+    mats = vt.gen_world(desc)
+    rng = np.random.default_rng(seed)
+    mats[rng.random(mats.shape) < 0.0005] = 9          # scattered floating voxels
+    w = vt.World(ctx, dims)
+    try:
+        w.upload_dense(mats)
+        b, c = w.distances()
+        hb, hc = host_fields(mats)
+        assert np.array_equal(c, hc)
+        for o in range(8):
+            bad = np.flatnonzero(b[o] != hb[o])
+            assert bad.size == 0, (o, bad[:8], b[o][bad[:8]], hb[o][bad[:8]])
+        assert (b > 1).mean() > 0.3 and (b == 0).any()
+    finally:
+        w.close()
+
+
 def test_pick_matches_oracle(vt, oracle, ctx):
     desc = vt.gen_desc((160, 96, 128), scale=0.6, seed=4, trees=40, caves=True)
     mats = vt.gen_world(desc)

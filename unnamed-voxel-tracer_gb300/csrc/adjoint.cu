@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_shade(AdjArgs a) {
     if (SMEM) {
         uint4* s_cd = reinterpret_cast<uint4*>(s_mem + 776);
         const uint4* src = reinterpret_cast<const uint4*>(a.w.cdist);
-        for (unsigned i = threadIdx.x; i < (a.w.nchunks + 15u) / 16u; i += blockDim.x) s_cd[i] = __ldg(src + i);
+        for (unsigned i = threadIdx.x; i < kOctants * a.w.cstride / 16u; i += blockDim.x) s_cd[i] = __ldg(src + i);
         cd = reinterpret_cast<const unsigned char*>(s_cd);
     }
     __syncthreads();
@@ -232,7 +232,7 @@ vt_status launch_shade(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
     a.kd = in->diffuse;
     a.shadow_steps = in->shadow_max_steps;
     const dim3 grid((cam->width + 15) / 16, (cam->height + 15) / 16);
-    const size_t dist_bytes = (size_t)((a.w.nchunks + 15u) / 16u) * 16u;
+    const size_t dist_bytes = (size_t)kOctants * a.w.cstride;
     const bool smem_dist = dist_bytes <= kMaxSharedDist;
     const size_t smem = 776 * sizeof(float) + (smem_dist ? dist_bytes : 0);
     if (bwd) {

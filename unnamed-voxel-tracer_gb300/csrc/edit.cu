@@ -152,13 +152,16 @@ vt_status vt_world_download_distances(vt_world* w, uint8_t* h_brick, size_t bric
                                       size_t chunk_bytes) {
     if (!w) return VT_ERR_ARG;
     const size_t nb = w->nchunks * kBricksPerChunk;
-    if (!h_brick || !h_chunk || brick_bytes != nb || chunk_bytes != w->nchunks)
-        return fail(w->ctx, VT_ERR_ARG, "distance download needs nchunks*512 and nchunks bytes");
+    if (!h_brick || !h_chunk || brick_bytes != kOctants * nb || chunk_bytes != kOctants * w->nchunks)
+        return fail(w->ctx, VT_ERR_ARG, "distance download needs 8*nchunks*512 and 8*nchunks bytes");
     cudaStream_t st = w->ctx->stream;
     vt_status s = update_distances(w, st);
     if (s) return s;
-    VT_CUDA(w->ctx, cudaMemcpyAsync(h_brick, w->d_bdist, nb, cudaMemcpyDeviceToHost, st));
-    VT_CUDA(w->ctx, cudaMemcpyAsync(h_chunk, w->d_cdist, w->nchunks, cudaMemcpyDeviceToHost, st));
+    VT_CUDA(w->ctx, cudaMemcpyAsync(h_brick, w->d_bdist, kOctants * nb, cudaMemcpyDeviceToHost, st));
+    const size_t cs = cdist_stride((unsigned)w->nchunks);
+    for (int o = 0; o < kOctants; ++o)
+        VT_CUDA(w->ctx, cudaMemcpyAsync(h_chunk + (size_t)o * w->nchunks, w->d_cdist + (size_t)o * cs, w->nchunks,
+                                        cudaMemcpyDeviceToHost, st));
     VT_CUDA(w->ctx, cudaStreamSynchronize(st));
     return VT_OK;
 }

@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kBlock, OCC ? 5 : 1) k_render(WorldView w, Fra
             for (unsigned i = threadIdx.x; i < w.ncoarse; i += blockDim.x) s_coarse[i] = __ldg(w.coarse + i);
         } else {
             const uint4* src = reinterpret_cast<const uint4*>(w.cdist);
-            for (unsigned i = threadIdx.x; i < (w.nchunks + 15u) / 16u; i += blockDim.x) s_dyn[i] = __ldg(src + i);
+            for (unsigned i = threadIdx.x; i < kOctants * w.cstride / 16u; i += blockDim.x) s_dyn[i] = __ldg(src + i);
         }
         __syncthreads();
     }
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kPersistBlock) k_render_persist(WorldView w, F
     const unsigned char* cd = w.cdist;
     if (SMEM) {
         const uint4* src = reinterpret_cast<const uint4*>(w.cdist);
-        for (unsigned i = threadIdx.x; i < (w.nchunks + 15u) / 16u; i += blockDim.x) s_dyn[i] = __ldg(src + i);
+        for (unsigned i = threadIdx.x; i < kOctants * w.cstride / 16u; i += blockDim.x) s_dyn[i] = __ldg(src + i);
         __syncthreads();
         cd = reinterpret_cast<const unsigned char*>(s_dyn);
     }
@@ -298,7 +298,7 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
     const WorldView w = world->view();
     const bool checked = (p->flags & VT_FLAG_CHECKED) != 0;
     const size_t smem = (stats || checked) ? (size_t)w.ncoarse * sizeof(unsigned long long)
-                                           : (size_t)((w.nchunks + 15u) / 16u) * 16u;
+                                           : (size_t)kOctants * w.cstride;
     const bool use_smem = smem <= kMaxSharedCoarse;
     {
         vt_status s = update_distances(const_cast<vt_world*>(world), stream);

@@ -269,9 +269,11 @@ __device__ __forceinline__ bool trace_p(const WorldView& w, const Coarse& coarse
 // The production traversal.  Same crossings, results and entry times as
 // trace_p (the jump argument holds for any empty axis-aligned box that contains
 // the current cell), with larger jumps and a cheaper unit step:
-//   - an empty chunk is left through the box of chunks within Chebyshev radius
-//     cdist - 1 (all empty), an empty brick through the box of bricks within
-//     radius bdist - 1;
+//   - an empty chunk is left through the box of chunks ahead within Chebyshev
+//     radius cdist - 1 (all empty), an empty brick through the box of bricks
+//     ahead within radius bdist - 1, both from the ray's octant field (the
+//     ray only moves forwards on every axis, so the exit of a box that extends
+//     forwards from the current unit is the exit of the symmetric box);
 //   - inside an occupied brick only the next-plane index nk and time tm of the
 //     crossing axis change; the crossed plane's index tells whether the step
 //     left the brick (k % 4 == 0), the chunk (k % 32 == 0) or the grid, and the
@@ -296,6 +298,7 @@ struct Walker {
     int axis;       // axis of the crossing that entered it
     unsigned long long word;
     unsigned wi, vb;
+    unsigned oct;   // direction octant: bit i set iff the ray moves towards +i
     int state;      // 0: chunk of c unknown; 1: brick of c unknown; 2: in the occupied brick `word`
 
     enum { kMore = 0, kHit = 1, kMiss = 2 };
@@ -314,6 +317,7 @@ struct Walker {
         n = 0;
         word = 0ull;
         wi = vb = 0;
+        oct = (r.pos[0] ? 1u : 0u) | (r.pos[1] ? 2u : 0u) | (r.pos[2] ? 4u : 0u);
         state = 0;
         return true;
     }
@@ -327,7 +331,7 @@ struct Walker {
 #pragma unroll
             for (int i = 0; i < 3; ++i) c[i] = r.pos[i] ? nk[i] - 1 : nk[i];
             const unsigned ci = (unsigned)(c[0] >> 5) + (unsigned)w.cdim[0] * ((unsigned)(c[1] >> 5) + (unsigned)w.cdim[1] * (unsigned)(c[2] >> 5));
-            const int dc = cdist[ci];
+            const int dc = cdist[oct * w.cstride + ci];
             if (dc) {
                 jump = true;
                 sh = 5;
@@ -345,7 +349,7 @@ struct Walker {
             if (word == 0ull) {
                 jump = true;
                 sh = 2;
-                rad = __ldg(w.bdist + wi);
+                rad = __ldg(w.bdist + (size_t)oct * w.nwords + wi);
             } else {
                 vb = (unsigned)(c[0] & 3) | ((unsigned)(c[1] & 3) << 2) | ((unsigned)(c[2] & 3) << 4);
                 state = 2;
@@ -391,14 +395,14 @@ struct Walker {
             else vb += dv;
             return kMore;
         }
-        // leave the empty box of radius rad - 1 units of 2^sh around the unit of c
+        // leave the empty box reaching rad - 1 units of 2^sh ahead of the unit of c
         VT_STEP_HOOK(sh == 5 ? 0 : 1);
         int K[3];
         float tK[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             const int u = c[i] >> sh;
-            // a brick distance d promises the box of radius d-1 across and
+            // a brick distance d promises d-1 bricks ahead across and
             // (d-1)/kFlatY vertically (kFlatY-weighted Chebyshev distance)
             const int ri = (i == 1 && sh == 2) ? (rad - 1) / kFlatY + 1 : rad;
             K[i] = r.pos[i] ? (u + ri) * (1 << sh) : (u - (ri - 1)) * (1 << sh);

@@ -28,9 +28,10 @@ struct WorldView {
     const unsigned char* mats;          // 64 material bytes per brick, same order
     const unsigned long long* coarse;   // one bit per chunk
     const unsigned* palette;            // 256 RGBA8
-    const unsigned char* bdist;         // per brick: 0 if occupied, else Chebyshev distance in bricks
-                                        // to the nearest occupied brick, capped at kDistCap + 1
-    const unsigned char* cdist;         // per chunk: same, in chunks
+    const unsigned char* bdist;         // kOctants fields of nwords bytes (octant-major), per brick:
+                                        // 0 if occupied, else the distance to the nearest occupied
+                                        // brick ahead in that octant (below), capped at kDistCap + 1
+    const unsigned char* cdist;         // kOctants fields of cstride bytes, per chunk: same, in chunks
     const float* entities;              // n_entities boxes {lo x, y, z, hi x, y, z}: shadow occluders
     int n_entities;
     int dims[3];
@@ -38,11 +39,22 @@ struct WorldView {
     unsigned nwords;                    // number of brick words
     unsigned ncoarse;                   // number of coarse words
     unsigned nchunks;
+    unsigned cstride;                   // bytes per chunk-distance field (nchunks rounded up to 16)
 };
 
 // Cap of the empty-space distances: a stored value d >= 1 promises that every
-// brick (chunk) within radius d - 1 is empty.
+// brick (chunk) within radius d - 1 ahead is empty.
 constexpr int kDistCap = 15;
+// Distances are kept per direction octant.  Field o (bit i set: the ray moves
+// towards +i) of a brick b holds min over occupied bricks b' with
+// sign(b'_i - b_i) in {0, that direction} of the weighted distance below: it
+// looks only where a ray of that octant can go.  A ray leaving b moves away
+// from b on every axis, so the empty box it may jump through only has to
+// extend forwards; rays that leave the terrain (shadow rays toward the sun,
+// primary rays above the ground) see the open space in front of them instead
+// of the terrain they came from.
+constexpr int kOctants = 8;
+__host__ __device__ inline unsigned cdist_stride(unsigned nchunks) { return (nchunks + 15u) / 16u * 16u; }
 // The brick distance weighs vertical offsets by kFlatY: d = min over occupied
 // bricks of max(|dx|, kFlatY*|dy|, |dz|).  Its empty box is flat and wide
 // (radius d-1 across, (d-1)/kFlatY up and down), which suits rays that skim
@@ -85,8 +97,8 @@ struct vt_world {
     unsigned* d_palette = nullptr;
     unsigned char* d_bdist = nullptr;
     unsigned char* d_cdist = nullptr;
-    unsigned char* d_dtmp = nullptr;   // x and y pass results of the brick distances (kept)
-    unsigned char* d_ctmp = nullptr;   // two chunk-sized buffers for the chunk distance passes
+    unsigned char* d_dtmp = nullptr;   // x (2 fields) and y (4 fields) pass results of the brick distances (kept)
+    unsigned char* d_ctmp = nullptr;   // the same 6 fields for the chunk distances
     int* d_edit = nullptr;             // {x, y, z, valid} of the last device-side edit
     float* d_entities = nullptr;       // kMaxEntities boxes of 6 floats
     int n_entities = 0;
@@ -114,6 +126,7 @@ struct vt_world {
         }
         v.nwords = (unsigned)(nchunks * vt::kBricksPerChunk);
         v.ncoarse = (unsigned)ncoarse;
+        v.cstride = vt::cdist_stride((unsigned)nchunks);
         return v;
     }
 };

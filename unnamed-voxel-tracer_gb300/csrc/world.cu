@@ -85,25 +85,32 @@ __global__ void __launch_bounds__(512) k_set_voxel(WorldView w, unsigned long lo
     }
 }
 
-// Empty-space distances.  The Chebyshev distance from a brick (chunk) to the
-// nearest occupied one is separable: min over b' of max(|dx|, |dy|, |dz|)
-// = min_dz max(|dz|, min_dy max(|dy|, min_dx max(|dx|, occ(b')))).  Each pass
-// is one of those 1-D min-max filters over a window of +-kDistCap; values are
-// capped at kDistCap + 1 ("nothing occupied within kDistCap").  Cells outside
-// the grid count as empty.
+// Empty-space distances, per direction octant.  For the octant with signs s,
+// the weighted Chebyshev distance from a brick (chunk) to the nearest
+// occupied one ahead is separable:
+//     min over b' ahead of max(|dx|, w|dy|, |dz|)
+//   = min_{dz ahead} max(|dz|, min_{dy ahead} max(w|dy|, min_{dx ahead} max(|dx|, occ(b')))),
+// "ahead" meaning 0 <= s_i * d_i <= kDistCap.  Each pass is one of those
+// one-sided 1-D min-max filters; values are capped at kDistCap + 1 ("nothing
+// occupied within kDistCap").  The x pass depends on s_x only (2 fields), the
+// y pass on s_x, s_y (4 fields), the z pass on all three (8 fields).  Cells
+// outside the grid count as empty.
 __device__ __forceinline__ unsigned brick_index(int bx, int by, int bz, int CX, int CY) {
     const unsigned ci = (unsigned)(bx >> 3) + (unsigned)CX * ((unsigned)(by >> 3) + (unsigned)CY * (unsigned)(bz >> 3));
     return ci * 512u + (unsigned)((bx & 7) | ((by & 7) << 3) | ((bz & 7) << 6));
 }
 
-// level 0: bricks (grid = 8 * chunk counts), level 1: chunks.  pass 0 reads
-// occupancy from the mask words / coarse bits, later passes read `in`.  The
-// pass covers the box [lo, lo + ext) of the grid (clipped to it); when
-// `d_cell` is given, {x, y, z, valid} of an edited voxel in device memory,
-// the box is taken relative to that voxel's brick and skipped when !valid.
+// level 0: bricks (grid = 8 * chunk counts), level 1: chunks.  blockIdx.y is
+// the output field v: bit i of v gives the direction of axis i (1: +) for
+// axes 0..axis; the pass reads input field v & ((1 << axis) - 1) (pass 0
+// reads the mask words / coarse bits instead).  Fields are `stride` bytes
+// apart.  The pass covers the box [lo, lo + ext) of the grid (clipped to it);
+// when `d_cell` is given, {x, y, z, valid} of an edited voxel in device
+// memory, the box is taken relative to that voxel's brick and skipped when
+// !valid.
 __global__ void k_dist_pass(const unsigned long long* __restrict__ mask, const unsigned long long* __restrict__ coarse,
                             const unsigned char* __restrict__ in, unsigned char* __restrict__ out, int level, int axis,
-                            int CX, int CY, int CZ, int3 lo, int3 ext, const int* __restrict__ d_cell) {
+                            int CX, int CY, int CZ, int3 lo, int3 ext, const int* __restrict__ d_cell, size_t stride) {
     const int gx = level == 0 ? CX * 8 : CX, gy = level == 0 ? CY * 8 : CY, gz = level == 0 ? CZ * 8 : CZ;
     if (d_cell) {
         if (!d_cell[3]) return;
@@ -111,6 +118,12 @@ __global__ void k_dist_pass(const unsigned long long* __restrict__ mask, const u
         lo.y += d_cell[1] >> 2;
         lo.z += d_cell[2] >> 2;
     }
+    const unsigned v = blockIdx.y;
+    const bool fwd = ((v >> axis) & 1u) != 0u;
+    if (axis > 0) in += (size_t)(v & ((1u << axis) - 1u)) * stride;
+    out += (size_t)v * stride;
+    const int dlo = fwd ? 0 : -kDistCap, dhi = fwd ? kDistCap : 0;
+    const int wgt = level == 0 && axis == 1 ? kFlatY : 1;
     const size_t total = (size_t)ext.x * ext.y * ext.z;
     for (size_t lin = blockIdx.x * (size_t)blockDim.x + threadIdx.x; lin < total; lin += (size_t)gridDim.x * blockDim.x) {
         const int x = lo.x + (int)(lin % ext.x), y = lo.y + (int)((lin / ext.x) % ext.y),
@@ -120,22 +133,21 @@ __global__ void k_dist_pass(const unsigned long long* __restrict__ mask, const u
         int p[3] = {x, y, z};
         const int u = p[axis];
         int best = kDistCap + 1;
-        for (int dd = -kDistCap; dd <= kDistCap; ++dd) {
+        for (int dd = dlo; dd <= dhi; ++dd) {
             const int q = u + dd;
             if (q < 0 || q >= g[axis]) continue;
             p[axis] = q;
             unsigned idx;
             if (level == 0) idx = brick_index(p[0], p[1], p[2], CX, CY);
             else idx = (unsigned)p[0] + (unsigned)CX * ((unsigned)p[1] + (unsigned)CY * (unsigned)p[2]);
-            int v;
+            int val;
             if (axis == 0) {
                 const bool occ = level == 0 ? mask[idx] != 0ull : ((coarse[idx >> 6] >> (idx & 63u)) & 1ull) != 0ull;
-                v = occ ? 0 : kDistCap + 1;
+                val = occ ? 0 : kDistCap + 1;
             } else {
-                v = in[idx];
+                val = in[idx];
             }
-            const int m = max((level == 0 && axis == 1 ? kFlatY : 1) * abs(dd), v);
-            best = min(best, m);
+            best = min(best, max(wgt * abs(dd), val));
         }
         p[axis] = u;
         const unsigned oidx = level == 0 ? brick_index(x, y, z, CX, CY)
@@ -152,30 +164,39 @@ unsigned dist_blocks(size_t n) {
     return (unsigned)std::min<size_t>((n + kDistThreads - 1) / kDistThreads, 65535u * 4u);
 }
 
-// The three chunk-level passes over the whole chunk grid (at most a few tens
-// of thousands of cells: cheap enough to redo after any edit).
-void chunk_passes(vt_world* w, cudaStream_t st) {
+// The three passes of one level over a box each: x into 2 fields of tmp, y
+// into the 4 fields after them, z into the 8 output fields.
+void level_passes(vt_world* w, cudaStream_t st, int level, unsigned char* tmp, unsigned char* out, size_t stride,
+                  const int3 lo[3], const int3 ext[3], const int* d_cell) {
     const int CX = w->cdim[0], CY = w->cdim[1], CZ = w->cdim[2];
-    unsigned char* a = w->d_ctmp;
-    unsigned char* b = w->d_ctmp + w->nchunks;
-    const int3 o = make_int3(0, 0, 0), g = make_int3(CX, CY, CZ);
-    k_dist_pass<<<dist_blocks(w->nchunks), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, nullptr, a, 1, 0, CX, CY, CZ, o, g, nullptr);
-    k_dist_pass<<<dist_blocks(w->nchunks), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, a, b, 1, 1, CX, CY, CZ, o, g, nullptr);
-    k_dist_pass<<<dist_blocks(w->nchunks), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, b, w->d_cdist, 1, 2, CX, CY, CZ, o, g, nullptr);
+    unsigned char* fx = tmp;
+    unsigned char* fy = tmp + 2 * stride;
+    auto grid = [&](int3 e, int fields) {
+        return dim3(dist_blocks((size_t)e.x * e.y * e.z), (unsigned)fields);
+    };
+    k_dist_pass<<<grid(ext[0], 2), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, nullptr, fx, level, 0, CX, CY, CZ,
+                                                         lo[0], ext[0], d_cell, stride);
+    k_dist_pass<<<grid(ext[1], 4), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, fx, fy, level, 1, CX, CY, CZ,
+                                                         lo[1], ext[1], d_cell, stride);
+    k_dist_pass<<<grid(ext[2], 8), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, fy, out, level, 2, CX, CY, CZ,
+                                                         lo[2], ext[2], d_cell, stride);
+}
+
+// The chunk level over the whole chunk grid (at most a few tens of thousands
+// of cells: cheap enough to redo after any edit).
+void chunk_passes(vt_world* w, cudaStream_t st) {
+    const int3 o = make_int3(0, 0, 0), g = make_int3(w->cdim[0], w->cdim[1], w->cdim[2]);
+    const int3 lo[3] = {o, o, o}, ext[3] = {g, g, g};
+    level_passes(w, st, 1, w->d_ctmp, w->d_cdist, cdist_stride((unsigned)w->nchunks), lo, ext, nullptr);
 }
 
 size_t volume(int3 e) { return (size_t)e.x * e.y * e.z; }
 
-// The brick passes: x into d_dtmp, y into d_dtmp + nbricks, z into d_bdist,
-// each over its own box.  The intermediates stay valid between calls, which
-// is what lets an edit recompute only the boxes it can change.
+// The brick level, each pass over its own box.  The intermediates stay valid
+// between calls, which is what lets an edit recompute only the boxes it can
+// change.
 void brick_passes(vt_world* w, cudaStream_t st, const int3 lo[3], const int3 ext[3], const int* d_cell) {
-    const int CX = w->cdim[0], CY = w->cdim[1], CZ = w->cdim[2];
-    unsigned char* bx = w->d_dtmp;
-    unsigned char* by = w->d_dtmp + w->nchunks * kBricksPerChunk;
-    k_dist_pass<<<dist_blocks(volume(ext[0])), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, nullptr, bx, 0, 0, CX, CY, CZ, lo[0], ext[0], d_cell);
-    k_dist_pass<<<dist_blocks(volume(ext[1])), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, bx, by, 0, 1, CX, CY, CZ, lo[1], ext[1], d_cell);
-    k_dist_pass<<<dist_blocks(volume(ext[2])), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, by, w->d_bdist, 0, 2, CX, CY, CZ, lo[2], ext[2], d_cell);
+    level_passes(w, st, 0, w->d_dtmp, w->d_bdist, w->nchunks * kBricksPerChunk, lo, ext, d_cell);
 }
 
 // After the bricks of box [blo, blo + bext) changed occupancy only these
@@ -308,10 +329,10 @@ vt_status vt_world_create(vt_ctx* ctx, const vt_world_desc* desc, vt_world** out
         (e = cudaMalloc(&w->d_mats, w->nchunks * (size_t)kChunkBytes)) != cudaSuccess ||
         (e = cudaMalloc(&w->d_coarse, w->ncoarse * 8)) != cudaSuccess ||
         (e = cudaMalloc(&w->d_palette, 256 * sizeof(unsigned))) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_bdist, w->nchunks * kBricksPerChunk)) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_cdist, (w->nchunks + 15) / 16 * 16)) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_dtmp, 2 * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_ctmp, 2 * w->nchunks)) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_bdist, kOctants * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_cdist, kOctants * (size_t)cdist_stride((unsigned)w->nchunks))) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_dtmp, 6 * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
+        (e = cudaMalloc(&w->d_ctmp, 6 * (size_t)cdist_stride((unsigned)w->nchunks))) != cudaSuccess ||
         (e = cudaMalloc(&w->d_edit, 4 * sizeof(int))) != cudaSuccess ||
         (e = cudaMalloc(&w->d_entities, kMaxEntities * 6 * sizeof(float))) != cudaSuccess ||
         (e = cudaMemset(w->d_edit, 0, 4 * sizeof(int))) != cudaSuccess ||

@@ -365,10 +365,11 @@ class World:
                                             d_out.ptr if d_out is not None else None, stream))
 
     def distances(self):
-        """(brick distances [nchunks*512], chunk distances [nchunks]) as uint8."""
+        """(brick distances [8, nchunks*512], chunk distances [8, nchunks]) as
+        uint8, one row per direction octant."""
         i = self.info()
         nch = i.chunks[0] * i.chunks[1] * i.chunks[2]
-        b, c = np.zeros(nch * 512, np.uint8), np.zeros(nch, np.uint8)
+        b, c = np.zeros((8, nch * 512), np.uint8), np.zeros((8, nch), np.uint8)
         self.ctx.check(self.ctx.lib.vt_world_download_distances(self.handle, _ptr(b), b.nbytes, _ptr(c), c.nbytes))
         return b, c
 
