@@ -25,7 +25,6 @@ namespace vt {
 namespace {
 
 constexpr int kAdjBlock = 256;
-constexpr size_t kMaxSharedDist = 48 * 1024;
 
 struct AdjArgs {
     WorldView w;
@@ -65,7 +64,7 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
-template <bool BWD, bool SMEM>
+template <bool BWD>
 __global__ void __launch_bounds__(kAdjBlock) k_shade(AdjArgs a) {
     extern __shared__ float s_mem[];
     float* s_gpal = s_mem;            // 768
@@ -73,12 +72,6 @@ __global__ void __launch_bounds__(kAdjBlock) k_shade(AdjArgs a) {
     const unsigned char* cd = a.w.cdist;
     if (BWD) {
         for (int i = threadIdx.x; i < 772; i += blockDim.x) s_mem[i] = 0.0f;
-    }
-    if (SMEM) {
-        uint4* s_cd = reinterpret_cast<uint4*>(s_mem + 776);
-        const uint4* src = reinterpret_cast<const uint4*>(a.w.cdist);
-        for (unsigned i = threadIdx.x; i < kOctants * a.w.cstride / 16u; i += blockDim.x) s_cd[i] = __ldg(src + i);
-        cd = reinterpret_cast<const unsigned char*>(s_cd);
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -232,16 +225,9 @@ vt_status launch_shade(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
     a.kd = in->diffuse;
     a.shadow_steps = in->shadow_max_steps;
     const dim3 grid((cam->width + 15) / 16, (cam->height + 15) / 16);
-    const size_t dist_bytes = (size_t)kOctants * a.w.cstride;
-    const bool smem_dist = dist_bytes <= kMaxSharedDist;
-    const size_t smem = 776 * sizeof(float) + (smem_dist ? dist_bytes : 0);
-    if (bwd) {
-        if (smem_dist) k_shade<true, true><<<grid, kAdjBlock, smem, st>>>(a);
-        else k_shade<true, false><<<grid, kAdjBlock, smem, st>>>(a);
-    } else {
-        if (smem_dist) k_shade<false, true><<<grid, kAdjBlock, smem, st>>>(a);
-        else k_shade<false, false><<<grid, kAdjBlock, smem, st>>>(a);
-    }
+    const size_t smem = 776 * sizeof(float);
+    if (bwd) k_shade<true><<<grid, kAdjBlock, smem, st>>>(a);
+    else k_shade<false><<<grid, kAdjBlock, smem, st>>>(a);
     VT_CUDA(ctx, cudaGetLastError());
     return VT_OK;
 }

@@ -42,18 +42,13 @@ struct BlockTile {
 template <bool STATS, bool CHECKED, bool SMEM, int TW, bool OCC>
 __global__ void __launch_bounds__(kBlock, OCC ? 5 : 1) k_render(WorldView w, FrameParams f, uint4* __restrict__ out,
                                                                unsigned* status, unsigned long long* counters) {
-    // shared copy of the coarse level: per-chunk distances (production) or
-    // coarse bits (model traversal)
+    // shared copy of the coarse bits for the model traversal (STATS or
+    // CHECKED); the production walk reads the chunk distances through L1,
+    // which measured faster than staging all 8 octant fields per block
     extern __shared__ uint4 s_dyn[];
     unsigned long long* s_coarse = reinterpret_cast<unsigned long long*>(s_dyn);
-    unsigned char* s_cdist = reinterpret_cast<unsigned char*>(s_dyn);
     if (SMEM) {
-        if (STATS || CHECKED) {
-            for (unsigned i = threadIdx.x; i < w.ncoarse; i += blockDim.x) s_coarse[i] = __ldg(w.coarse + i);
-        } else {
-            const uint4* src = reinterpret_cast<const uint4*>(w.cdist);
-            for (unsigned i = threadIdx.x; i < kOctants * w.cstride / 16u; i += blockDim.x) s_dyn[i] = __ldg(src + i);
-        }
+        for (unsigned i = threadIdx.x; i < w.ncoarse; i += blockDim.x) s_coarse[i] = __ldg(w.coarse + i);
         __syncthreads();
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -65,7 +60,7 @@ __global__ void __launch_bounds__(kBlock, OCC ? 5 : 1) k_render(WorldView w, Fra
     for (int k = 0; k < kNumCounters; ++k) pc.v[k] = 0;
     if (px < f.width && py < f.height) {
         uint4 rec;
-        if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, s_cdist, f, px, py, status, pc);
+        if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, w.cdist, f, px, py, status, pc);
         else rec = render_pixel<STATS, CHECKED>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, status, pc);
         out[(size_t)py * f.width + px] = rec;
     }
@@ -89,7 +84,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_rays(WorldView w, const float*
     pray_init(r, o, d);
     TraceHit h;
     TraceCounters cnt;
-    const bool hit = trace_fast<true>(w, w.cdist, r, max_steps, h);
+    const bool hit = trace_fast<true, true>(w, w.cdist, r, max_steps, h);
     if (hit) {
         const int e = h.axis;
         const bool pe = e == 0 ? r.pos[0] : (e == 1 ? r.pos[1] : r.pos[2]);
@@ -102,7 +97,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_rays(WorldView w, const float*
 }
 
 // ---------------------------------------------------------------------------
-// Persistent render kernel (production path).
+// Persistent render kernel (a tuning option: VT_KERNEL_QUEUE).
 //
 // A one-ray-per-thread launch leaves lanes idle: a warp runs until its longest
 // primary ray ends, then again until its longest shadow ray ends, while lanes
@@ -121,18 +116,10 @@ __device__ __forceinline__ void pixel_of(unsigned idx, unsigned tiles_x, int& px
     py = (int)((tile / tiles_x) * 4u + (l >> 3));
 }
 
-template <bool SMEM>
 __global__ void __launch_bounds__(kPersistBlock) k_render_persist(WorldView w, FrameParams f, uint4* __restrict__ out,
                                                                   unsigned* __restrict__ work, unsigned total,
                                                                   unsigned tiles_x, int batch) {
-    extern __shared__ uint4 s_dyn[];
     const unsigned char* cd = w.cdist;
-    if (SMEM) {
-        const uint4* src = reinterpret_cast<const uint4*>(w.cdist);
-        for (unsigned i = threadIdx.x; i < kOctants * w.cstride / 16u; i += blockDim.x) s_dyn[i] = __ldg(src + i);
-        __syncthreads();
-        cd = reinterpret_cast<const unsigned char*>(s_dyn);
-    }
     const unsigned lane = threadIdx.x & 31u;
     const unsigned below = (1u << lane) - 1u;
     unsigned bnext = 0, bend = 0;  // the warp's batch of queue entries (warp-uniform)
@@ -297,9 +284,8 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
     const FrameParams f = make_frame(cam, p);
     const WorldView w = world->view();
     const bool checked = (p->flags & VT_FLAG_CHECKED) != 0;
-    const size_t smem = (stats || checked) ? (size_t)w.ncoarse * sizeof(unsigned long long)
-                                           : (size_t)kOctants * w.cstride;
-    const bool use_smem = smem <= kMaxSharedCoarse;
+    const size_t smem = (size_t)w.ncoarse * sizeof(unsigned long long);
+    const bool use_smem = (stats || checked) && smem <= kMaxSharedCoarse;
     {
         vt_status s = update_distances(const_cast<vt_world*>(world), stream);
         if (s) return s;
@@ -311,8 +297,7 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         // of the context's ring, zeroed on this stream before the launch
         if (ctx->persist_blocks == 0) {
             int nb = 0;
-            VT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_render_persist<true>, kPersistBlock,
-                                                                      kMaxSharedCoarse));
+            VT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_render_persist, kPersistBlock, 0));
             ctx->persist_blocks = nb > 0 ? nb : 1;
         }
         unsigned* counter = ctx->d_work + (ctx->work_slot++ % kWorkSlots);
@@ -321,10 +306,7 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         const unsigned total = tiles_x * tiles_y * 32u;
         const unsigned blocks = (unsigned)(ctx->sm_count * ctx->persist_blocks);
         const int batch = tu.batch;
-        if (use_smem)
-            k_render_persist<true><<<blocks, kPersistBlock, sm, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
-        else
-            k_render_persist<false><<<blocks, kPersistBlock, 0, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
+        k_render_persist<<<blocks, kPersistBlock, 0, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
         VT_CUDA(ctx, cudaGetLastError());
         return VT_OK;
     }
@@ -340,14 +322,14 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
     } else if (checked) {
         VT_LAUNCH_M(false, true, 8, false);
     } else if (tu.warp_tile_w == 16) {
-        if (tu.occupancy) { VT_LAUNCH_M(false, false, 16, true); }
-        else { VT_LAUNCH_M(false, false, 16, false); }
+        if (tu.occupancy) { VT_LAUNCH(false, false, false, 16, true); }
+        else { VT_LAUNCH(false, false, false, 16, false); }
     } else if (tu.warp_tile_w == 32) {
-        if (tu.occupancy) { VT_LAUNCH_M(false, false, 32, true); }
-        else { VT_LAUNCH_M(false, false, 32, false); }
+        if (tu.occupancy) { VT_LAUNCH(false, false, false, 32, true); }
+        else { VT_LAUNCH(false, false, false, 32, false); }
     } else {
-        if (tu.occupancy) { VT_LAUNCH_M(false, false, 8, true); }
-        else { VT_LAUNCH_M(false, false, 8, false); }
+        if (tu.occupancy) { VT_LAUNCH(false, false, false, 8, true); }
+        else { VT_LAUNCH(false, false, false, 8, false); }
     }
 #undef VT_LAUNCH_M
 #undef VT_LAUNCH

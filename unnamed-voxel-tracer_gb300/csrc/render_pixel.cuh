@@ -15,12 +15,12 @@ struct PixelCounters {
 // The instrumented and bounds-checked variants run the three-level model
 // traversal (it defines the algorithmic byte counts); the production variant
 // runs trace_fast.  Both give identical results.
-template <bool STATS, bool CHECKED, bool MAT, class Coarse>
+template <bool STATS, bool CHECKED, bool MAT, bool RUN, class Coarse>
 __device__ __forceinline__ bool trace_any(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
                                           const PRay& r, int max_steps, TraceHit& h, TraceCounters& cnt,
                                           unsigned* status) {
     if (STATS || CHECKED) return trace_p<STATS, CHECKED, MAT>(w, coarse, r, max_steps, h, cnt, status);
-    return trace_fast<MAT>(w, cd, r, max_steps, h);
+    return trace_fast<MAT, RUN>(w, cd, r, max_steps, h);
 }
 
 template <bool STATS, bool CHECKED, class Coarse>
@@ -33,7 +33,7 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
     pray_init(r, o, d);
     TraceHit h;
     TraceCounters cnt;
-    const bool hit = trace_any<STATS, CHECKED, true>(w, coarse, cd, r, f.max_steps, h, cnt, status);
+    const bool hit = trace_any<STATS, CHECKED, true, true>(w, coarse, cd, r, f.max_steps, h, cnt, status);
     if (STATS) {
         pc.v[0] += 1;
         pc.v[9] += 16;
@@ -66,7 +66,7 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
             PRay rs;
             pray_init(rs, so, f.sun);
             TraceHit hs;
-            shadowed = trace_any<STATS, CHECKED, false>(w, coarse, cd, rs, f.shadow_max_steps, hs, cnt, status);
+            shadowed = trace_any<STATS, CHECKED, false, true>(w, coarse, cd, rs, f.shadow_max_steps, hs, cnt, status);
             if (shadowed) flags |= VT_HIT_SHADOWED;
             if (STATS) {
                 pc.v[2] += 1;
@@ -85,7 +85,7 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
             PRay rb;
             pray_init(rb, so, bdir);
             TraceHit hb;
-            const bool bh = trace_any<STATS, CHECKED, false>(w, coarse, cd, rb, f.bounce_max_steps, hb, cnt, status);
+            const bool bh = trace_any<STATS, CHECKED, false, true>(w, coarse, cd, rb, f.bounce_max_steps, hb, cnt, status);
             if (bh) flags |= VT_HIT_BOUNCE;
             bounce_open = !bh;
             if (STATS) {

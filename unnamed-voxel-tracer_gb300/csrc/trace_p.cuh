@@ -322,8 +322,13 @@ struct Walker {
         return true;
     }
 
-    // One iteration: a lookup plus a jump, or a voxel test plus a unit step.
-    template <bool MAT>
+    // One iteration: a lookup plus a jump, or a voxel test plus a unit step
+    // (RUN: unit steps until the walk leaves the occupied brick).  In a warp
+    // whose lanes are in different phases every iteration pays for both the
+    // jump and the unit-step code; running a lane's unit steps in one inner
+    // loop pays the jump code once per brick visit instead (-4.5% on a 1080p
+    // terrain frame of primary and shadow rays).
+    template <bool MAT, bool RUN = true>
     __device__ __forceinline__ int step(const WorldView& w, const unsigned char* cdist, TraceHit& h) {
         bool jump = false;
         int sh = 0, rad = 0;
@@ -356,6 +361,7 @@ struct Walker {
             }
         }
         if (!jump) {
+          for (;;) {
             // inside an occupied brick: test the voxel, else one unit crossing
             VT_STEP_HOOK(2);
             const unsigned half = (vb & 32u) ? (unsigned)(word >> 32) : (unsigned)word;
@@ -391,9 +397,13 @@ struct Walker {
             axis = e;
             ++n;
             if (n >= max_steps || k == xp) return kMiss;
-            if ((k & 3) == 0) state = (k & 31) == 0 ? 0 : 1;
-            else vb += dv;
-            return kMore;
+            if ((k & 3) == 0) {
+                state = (k & 31) == 0 ? 0 : 1;
+                return kMore;
+            }
+            vb += dv;
+            if (!RUN) return kMore;
+          }
         }
         // leave the empty box reaching rad - 1 units of 2^sh ahead of the unit of c
         VT_STEP_HOOK(sh == 5 ? 0 : 1);
@@ -433,13 +443,13 @@ struct Walker {
     }
 };
 
-template <bool MAT>
+template <bool MAT, bool RUN = true>
 __device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned char* cdist, const PRay& r,
                                            int max_steps, TraceHit& h) {
     Walker wk;
     if (!wk.start(w, r.o, r.d, max_steps)) return false;
     int s;
-    while ((s = wk.step<MAT>(w, cdist, h)) == Walker::kMore) {
+    while ((s = wk.step<MAT, RUN>(w, cdist, h)) == Walker::kMore) {
     }
     return s == Walker::kHit;
 }
