@@ -134,6 +134,30 @@ def test_repeated_frames_are_identical(vt, tuned):
     w.close()
 
 
+@pytest.mark.parametrize("tw", [8, 16, 32])
+def test_render_host_pipeline_equals_device_render(vt, tuned, tw):
+    """Frames of >= 2^18 pixels go through vt_render_host's row-band pipeline
+    (bands on several streams, each copied out when done); the records equal
+    one device-side vt_render of the frame."""
+    d = vt.gen_desc((256, 128, 256), seed=6, trees=40)
+    w = make_world(vt, tuned, vt.gen_world(d))
+    tuned.set_tuning(kernel=0, warp_tile_w=tw, occupancy=1)
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=vt.gen_sun(6))
+    try:
+        for cs, (W, H) in enumerate([(1280, 720), (701, 397), (512, 1031)]):
+            cam = vt.gen_camera(d, cs, W, H)
+            buf = tuned.alloc(W * H * 16)
+            vt.render(tuned, w, cam, p, buf)
+            tuned.sync()
+            want = buf.download(np.zeros(W * H, vt.HIT_DTYPE))
+            buf.free()
+            got = vt.render_host(tuned, w, cam, p)
+            assert np.array_equal(got, want), (W, H)
+            assert (got["face"] != 0xFF).sum() > 1000
+    finally:
+        w.close()
+
+
 def test_autotune_picks_a_candidate_and_caches_it(vt, tuned, tmp_path):
     d = vt.gen_desc((256, 128, 256), seed=5, trees=20)
     w = make_world(vt, tuned, vt.gen_world(d))

@@ -100,6 +100,17 @@ vt_status vt_ctx_destroy(vt_ctx* ctx) {
     if (!ctx) return VT_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    for (int i = 0; i < kBandStreams; ++i)
+        if (ctx->band_stream[i]) {
+            cudaStreamSynchronize(ctx->band_stream[i]);
+            cudaStreamDestroy(ctx->band_stream[i]);
+        }
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+    if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
+    for (int i = 0; i < kMaxBands; ++i)
+        if (ctx->ev_band[i]) cudaEventDestroy(ctx->ev_band[i]);
     if (ctx->d_scratch) cudaFree(ctx->d_scratch);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->d_counters) cudaFree(ctx->d_counters);

@@ -54,11 +54,11 @@ __global__ void __launch_bounds__(kBlock, OCC ? 5 : 1) k_render(WorldView w, Fra
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     using BT = BlockTile<TW>;
     const int px = blockIdx.x * BT::kW + (warp % BT::kWarpsX) * TW + (lane % TW);
-    const int py = blockIdx.y * BT::kH + (warp / BT::kWarpsX) * (32 / TW) + (lane / TW);
+    const int py = f.row0 + blockIdx.y * BT::kH + (warp / BT::kWarpsX) * (32 / TW) + (lane / TW);
     PixelCounters pc;
 #pragma unroll
     for (int k = 0; k < kNumCounters; ++k) pc.v[k] = 0;
-    if (px < f.width && py < f.height) {
+    if (px < f.width && py < f.row_end) {
         uint4 rec;
         if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, w.cdist, f, px, py, status, pc);
         else rec = render_pixel<STATS, CHECKED>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, status, pc);
@@ -108,6 +108,11 @@ __global__ void __launch_bounds__(kBlock) k_trace_rays(WorldView w, const float*
 // the batch is used up.  Queue entries walk the image in 8 x 4 pixel tiles, so
 // the lanes of a warp still trace neighbouring pixels.
 constexpr int kPersistBlock = 128;
+// vt_render_host splits frames of at least kPipelinePixels into
+// kPipelineBands row bands (at most kMaxBands).
+constexpr size_t kPipelinePixels = 1u << 18;
+constexpr int kPipelineBands = 8;
+static_assert(kPipelineBands <= kMaxBands, "band events");
 constexpr unsigned kGrab = 32;
 
 __device__ __forceinline__ void pixel_of(unsigned idx, unsigned tiles_x, int& px, int& py) {
@@ -255,6 +260,8 @@ FrameParams make_frame(const vt_camera* cam, const vt_params* p) {
     f.tan_half_fov = cam->tan_half_fov;
     f.width = cam->width;
     f.height = cam->height;
+    f.row0 = 0;
+    f.row_end = cam->height;
     f.max_steps = p->max_steps;
     f.shadow_max_steps = p->shadow_max_steps;
     f.bounce_max_steps = p->bounce_max_steps;
@@ -279,9 +286,33 @@ vt_status check_frame_args(vt_ctx* ctx, const vt_world* world, const vt_camera* 
     return VT_OK;
 }
 
+// Height in rows of the block tile of the production kernel for a tuning
+// (bands of vt_render_host are multiples of it); 0 for the queue kernel.
+int band_rows_unit(const vt_tuning& tu) {
+    if (tu.kernel != VT_KERNEL_TILE) return 0;
+    if (tu.warp_tile_w == 16) return BlockTile<16>::kH;
+    if (tu.warp_tile_w == 32) return BlockTile<32>::kH;
+    return BlockTile<8>::kH;
+}
+
+vt_status band_streams(vt_ctx* ctx) {
+    if (ctx->copy_stream) return VT_OK;
+    for (int i = 0; i < kBandStreams; ++i)
+        VT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->band_stream[i], cudaStreamNonBlocking));
+    VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_start, cudaEventDisableTiming));
+    VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming));
+    for (int i = 0; i < kMaxBands; ++i) VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_band[i], cudaEventDisableTiming));
+    VT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    return VT_OK;
+}
+
 vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p,
-                               uint4* d_out, cudaStream_t stream, bool stats) {
-    const FrameParams f = make_frame(cam, p);
+                               uint4* d_out, cudaStream_t stream, bool stats, int row0, int row1) {
+    FrameParams f = make_frame(cam, p);
+    if (row1 < 0) row1 = cam->height;
+    f.row0 = row0;
+    f.row_end = row1;
+    const int rows = row1 - row0;
     const WorldView w = world->view();
     const bool checked = (p->flags & VT_FLAG_CHECKED) != 0;
     const size_t smem = (size_t)w.ncoarse * sizeof(unsigned long long);
@@ -312,7 +343,7 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
     }
 #define VT_LAUNCH(S, C, M, TW, O)                                                                               \
     k_render<S, C, M, TW, O><<<dim3((cam->width + BlockTile<TW>::kW - 1) / BlockTile<TW>::kW,                   \
-                                    (cam->height + BlockTile<TW>::kH - 1) / BlockTile<TW>::kH),                 \
+                                    (rows + BlockTile<TW>::kH - 1) / BlockTile<TW>::kH),                        \
                                kBlock, sm, stream>>>(w, f, d_out, ctx->d_status, ctx->d_counters)
 #define VT_LAUNCH_M(S, C, TW, O)      \
     if (use_smem) VT_LAUNCH(S, C, true, TW, O); \
@@ -375,13 +406,51 @@ vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* ca
     vt_status s = check_frame_args(ctx, world, cam, params);
     if (s) return s;
     if (!h_out) return fail(ctx, VT_ERR_ARG, "null output buffer");
-    const size_t bytes = (size_t)cam->width * cam->height * sizeof(vt_hit);
-    void* d_out = nullptr;
-    s = ctx_scratch(ctx, bytes, &d_out);
+    const size_t W = (size_t)cam->width, H = (size_t)cam->height;
+    const size_t bytes = W * H * sizeof(vt_hit);
+    void* d_scratch = nullptr;
+    s = ctx_scratch(ctx, bytes, &d_scratch);
     if (s) return s;
-    s = launch_render(ctx, world, cam, params, reinterpret_cast<uint4*>(d_out), ctx->stream, false);
+    uint4* d_out = reinterpret_cast<uint4*>(d_scratch);
+    const int rows_tile = band_rows_unit(ctx->tuning);
+    const bool pipelined = ctx->tuning.kernel == VT_KERNEL_TILE && W * H >= kPipelinePixels &&
+                           (params->flags & VT_FLAG_CHECKED) == 0 && rows_tile > 0;
+    if (!pipelined) {
+        s = launch_render(ctx, world, cam, params, d_out, ctx->stream, false);
+        if (s) return s;
+        VT_CUDA(ctx, cudaMemcpyAsync(h_out, d_out, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        return vt_sync(ctx, ctx->stream);
+    }
+    // Row bands, rendered on kBandStreams streams (so that one band's tail
+    // overlaps the next band) and copied to the host each as soon as it is
+    // done: the copy of the frame overlaps its rendering, except the last band.
+    s = band_streams(ctx);
     if (s) return s;
-    VT_CUDA(ctx, cudaMemcpyAsync(h_out, d_out, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    s = update_distances(const_cast<vt_world*>(world), ctx->stream);
+    if (s) return s;
+    VT_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+    for (int i = 0; i < kBandStreams; ++i) VT_CUDA(ctx, cudaStreamWaitEvent(ctx->band_stream[i], ctx->ev_start, 0));
+    const int bands = (int)std::min<size_t>(kPipelineBands, (H + rows_tile - 1) / rows_tile);
+    const int per = (int)(((H + bands - 1) / bands + rows_tile - 1) / rows_tile) * rows_tile;
+    int nb = 0;
+    for (int r0 = 0; r0 < (int)H; r0 += per, ++nb) {
+        const int r1 = std::min((int)H, r0 + per);
+        cudaStream_t bs = ctx->band_stream[nb % kBandStreams];
+        s = launch_render(ctx, world, cam, params, d_out, bs, false, r0, r1);
+        if (s) return s;
+        VT_CUDA(ctx, cudaEventRecord(ctx->ev_band[nb], bs));
+    }
+    // copies queued after every launch: with pageable host memory a copy
+    // returns only when done, and must not hold back the launches
+    nb = 0;
+    for (int r0 = 0; r0 < (int)H; r0 += per, ++nb) {
+        const int r1 = std::min((int)H, r0 + per);
+        VT_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_band[nb], 0));
+        VT_CUDA(ctx, cudaMemcpyAsync(h_out + (size_t)r0 * W, d_out + (size_t)r0 * W, (size_t)(r1 - r0) * W * sizeof(vt_hit),
+                                     cudaMemcpyDeviceToHost, ctx->copy_stream));
+    }
+    VT_CUDA(ctx, cudaEventRecord(ctx->ev_done, ctx->copy_stream));
+    VT_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_done, 0));
     return vt_sync(ctx, ctx->stream);
 }
 

@@ -30,6 +30,7 @@ struct FrameParams {
     float sun_n[3];     // normalised sun direction
     float lit_sky[3];   // SkyDome2 of the RGBA8-stored sun direction (blit.fragment.glsl:31)
     float lit_a;        // illumination alpha 0.3 stored in RGBA8
+    int row0, row_end;  // rows [row0, row_end) of the image this launch renders
 };
 
 __device__ __forceinline__ void primary_ray(const FrameParams& f, int px, int py, float o[3], float d[3]) {

@@ -79,10 +79,19 @@ struct vt_ctx {
     unsigned work_slot = 0;
     int persist_blocks = 0;                      // resident blocks per SM of the persistent render kernel
     vt_tuning tuning = {VT_KERNEL_TILE, 8, 1, 16};
+    // vt_render_host's pipeline: row bands rendered on band streams, each
+    // copied to the host on the copy stream as soon as it is done (created on
+    // first use)
+    cudaStream_t band_stream[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_band[16] = {};
 };
 
 namespace vt {
 constexpr int kWorkSlots = 256;
+constexpr int kBandStreams = 4;
+constexpr int kMaxBands = 16;
 }
 
 struct vt_world {
@@ -154,7 +163,7 @@ vt_status check_frame_args(vt_ctx* ctx, const vt_world* world, const vt_camera* 
 // Queues one frame (render kernel, distances rebuilt first if stale) writing
 // width*height records to d_out on `stream`.
 vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p, uint4* d_out,
-                        cudaStream_t stream, bool stats);
+                        cudaStream_t stream, bool stats, int row0 = 0, int row1 = -1);
 }  // namespace vt
 
 #define VT_CUDA(ctx, call)                                                      \
