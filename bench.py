@@ -241,7 +241,9 @@ def measure_config2(vt, scenes, ctx, torch, flush) -> dict:
 
 def measure_config3(vt, scenes, ctx, torch) -> dict:
     """64 cube scenes (edge log-uniform in [32, 512]) x 1-8 cameras: one
-    persistent CUDA-graph launch vs one vt_render launch per camera."""
+    CUDA-graph launch of the batch vs one vt_render launch per camera.  The
+    default batch graph holds the per-camera launches on 8 concurrent chains;
+    the queue shape (one persistent kernel over 16x16 units) is timed too."""
     sc, params = scenes.config3()
     worlds, jobs = [], []
     for desc, cams in sc:
@@ -263,6 +265,12 @@ def measure_config3(vt, scenes, ctx, torch) -> dict:
     t_batch = _timed(torch, lambda: batch.launch(sh), 3)
     pixels = batch.info()["pixels"]
     batch.close()
+    ctx.set_tuning(kernel=vt.KERNEL_QUEUE)
+    qbatch = vt.Batch(ctx, jobs, params)
+    qbatch.launch(sh)
+    ctx.set_tuning()
+    t_queue = _timed(torch, lambda: qbatch.launch(sh), 3)
+    qbatch.close()
     for _, _, buf in jobs:
         buf.free()
     for w in worlds:
@@ -271,6 +279,7 @@ def measure_config3(vt, scenes, ctx, torch) -> dict:
             "batched_gpix_per_s": pixels / (t_batch * 1e-3) / 1e9,
             "per_scene_gpix_per_s": pixels / (t_scene * 1e-3) / 1e9,
             "batched_ms": t_batch, "per_scene_ms": t_scene, "speedup": t_scene / t_batch,
+            "batched_queue_gpix_per_s": pixels / (t_queue * 1e-3) / 1e9,
             "launches_per_scene_path": len(jobs)}
 
 

@@ -312,9 +312,11 @@ vt_status vt_brickmap_edit(vt_ctx* ctx, vt_brickmap* bm, const vt_camera* cam, i
                            vt_stream stream);
 
 /* ----------------------------------------------------------------- batch
- * Many scenes x cameras in one launch (no counterpart in the reference, which
- * renders one camera per frame, game.zig:232-256).  A persistent kernel pulls
- * 16x16-pixel units of all jobs from one device work queue; every job's
+ * Many scenes x cameras in one graph launch (no counterpart in the reference,
+ * which renders one camera per frame, game.zig:232-256).  Under the default
+ * tuning the graph holds one render launch per job on eight concurrent
+ * chains; under VT_KERNEL_QUEUE it holds one persistent kernel that pulls
+ * 16x16-pixel units of all jobs from a device work queue.  Every job's
  * records are identical to what vt_render writes for it alone. */
 typedef struct {
     const vt_world* world;
@@ -323,8 +325,9 @@ typedef struct {
 } vt_job;
 
 /* Uploads the job table and sizes the launch.  The batch is replayed with
- * vt_batch_launch, which captures a CUDA graph (queue reset + kernel) on its
- * first call and launches that graph on the given stream every time. */
+ * vt_batch_launch, which captures a CUDA graph on its first call (with the
+ * context's tuning at that moment) and launches that graph on the given
+ * stream every time. */
 vt_status vt_batch_create(vt_ctx* ctx, const vt_job* jobs, int32_t n, const vt_params* params, vt_batch** out);
 vt_status vt_batch_launch(vt_batch* batch, vt_stream stream);
 vt_status vt_batch_destroy(vt_batch* batch);

@@ -1,14 +1,16 @@
-"""The batched persistent launch (vt_batch_*): many worlds of different sizes,
-several cameras each at different resolutions, one CUDA-graph launch.  Every
-job's records must equal what vt_render writes for that job alone (and hence
-the oracle's, which test_gpu_render checks for vt_render)."""
+"""The batched launch (vt_batch_*): many worlds of different sizes, several
+cameras each at different resolutions, one CUDA-graph launch, in both shapes
+(per-job launches on concurrent graph chains; one persistent unit-queue
+kernel).  Every job's records must equal what vt_render writes for that job
+alone (and hence the oracle's, which test_gpu_render checks for vt_render)."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 
-def test_batch_matches_per_job_renders(vt, ctx, oracle):
+@pytest.mark.parametrize("kernel", [0, 1], ids=["tile-graph", "queue"])
+def test_batch_matches_per_job_renders(vt, ctx, oracle, kernel):
     rng = np.random.default_rng(31)
     worlds, jobs, outs = [], [], []
     params = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=vt.gen_sun(31))
@@ -26,15 +28,20 @@ def test_batch_matches_per_job_renders(vt, ctx, oracle):
     batch = vt.Batch(ctx, jobs, params)
     info = batch.info()
     assert info["jobs"] == len(jobs)
-    for rep in range(3):   # graph replays reuse the queue counter
-        for _, cam, buf in jobs:
-            buf.zero()
-        batch.launch()
-        ctx.sync()
-        for w, cam, buf in jobs:
-            got = buf.download(np.zeros(cam.width * cam.height, vt.HIT_DTYPE))
-            want = vt.render_host(ctx, w, cam, params)
-            assert np.array_equal(got, want)
+    try:
+        ctx.set_tuning(kernel=kernel)        # the graph is captured at the first launch
+        for rep in range(3):   # graph replays reuse the queue counter
+            for _, cam, buf in jobs:
+                buf.zero()
+            batch.launch()
+            ctx.sync()
+            ctx.set_tuning()
+            for w, cam, buf in jobs:
+                got = buf.download(np.zeros(cam.width * cam.height, vt.HIT_DTYPE))
+                want = vt.render_host(ctx, w, cam, params)
+                assert np.array_equal(got, want)
+    finally:
+        ctx.set_tuning()
     batch.close()
     for _, _, buf in jobs:
         buf.free()

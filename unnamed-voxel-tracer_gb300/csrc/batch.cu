@@ -1,14 +1,22 @@
-// batch.cu -- many scenes x cameras in one persistent launch.
+// batch.cu -- many scenes x cameras in one graph launch.
 //
-// Every job (a world, a camera, an output buffer) is cut into 16 x 16 pixel
-// units; the units of all jobs are numbered consecutively, job after job.  A
-// persistent grid (SMs x resident blocks) runs until a device counter hands out
-// the last unit: a warp takes one unit at a time, finds its job by binary
-// search over the jobs' first-unit numbers, and traces the unit's 256 pixels as
-// eight 8 x 4 tiles, one pixel per lane, with the same per-pixel code as the
-// single-frame kernel (render_pixel.cuh).  Large and small frames of worlds of
-// very different sizes therefore share the GPU without per-launch tails, and
-// the whole batch is one CUDA graph launch (counter reset + kernel).
+// A batch (jobs of a world, a camera and an output buffer each) is captured
+// once into a CUDA graph and replayed with one cudaGraphLaunch.  Two shapes:
+//
+//   tile (default)  one production k_render launch per job, spread over
+//                   kBatchChains independent chains of the graph, so that the
+//                   tail of one job's launch overlaps the next jobs' work and
+//                   every launch keeps its world and frame in kernel
+//                   parameters (constant bank) as the single-frame path does.
+//   queue           (ctx tuning VT_KERNEL_QUEUE) one persistent launch: every
+//                   job is cut into 16 x 16 pixel units numbered job after
+//                   job; a warp takes one unit at a time from a device
+//                   counter, finds its job by binary search over the jobs'
+//                   first-unit numbers and traces the unit's 256 pixels as
+//                   eight 8 x 4 tiles with the same per-pixel code
+//                   (render_pixel.cuh).  Its per-job state comes from global
+//                   memory, which measured slower than the tile shape once
+//                   the traversal itself got cheaper.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -27,6 +35,7 @@ struct JobDesc {
 
 constexpr int kBatchBlock = 256;
 constexpr int kUnit = 16;  // pixels per unit side
+constexpr int kBatchChains = 8;
 
 __global__ void __launch_bounds__(kBatchBlock, 4) k_render_batch(const JobDesc* __restrict__ jobs, int njobs,
                                                                  unsigned total_units, unsigned* __restrict__ counter) {
@@ -64,6 +73,8 @@ __global__ void __launch_bounds__(kBatchBlock, 4) k_render_batch(const JobDesc* 
 struct vt_batch {
     vt_ctx* ctx = nullptr;
     std::vector<const vt_world*> worlds;
+    std::vector<vt_job> jobs;
+    vt_params params;
     vt::JobDesc* d_jobs = nullptr;
     unsigned* d_counter = nullptr;
     int njobs = 0;
@@ -103,7 +114,9 @@ vt_status vt_batch_create(vt_ctx* ctx, const vt_job* jobs, int32_t n, const vt_p
         units += (unsigned long long)d.units_x * (unsigned)((j.camera.height + kUnit - 1) / kUnit);
         pixels += (unsigned long long)j.camera.width * (unsigned long long)j.camera.height;
         b->worlds.push_back(j.world);
+        b->jobs.push_back(j);
     }
+    b->params = *params;
     if (units >= (1ull << 32)) {
         delete b;
         return fail(ctx, VT_ERR_ARG, "batch too large (units >= 2^32)");
@@ -139,16 +152,47 @@ vt_status vt_batch_launch(vt_batch* b, vt_stream stream) {
         if (s) return s;
     }
     if (!b->exec) {
-        // capture on a private stream: the legacy default stream cannot be captured
+        // capture on private streams: the legacy default stream cannot be captured
         cudaStream_t cap = nullptr;
-        VT_CUDA(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), cap);
-            k_render_batch<<<b->blocks, kBatchBlock, 0, cap>>>(b->d_jobs, b->njobs, b->total_units, b->d_counter);
-            e = cudaStreamEndCapture(cap, &b->graph);
+        cudaStream_t chain[kBatchChains] = {};
+        cudaEvent_t fork = nullptr, join[kBatchChains] = {};
+        cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+        const bool queue = ctx->tuning.kernel == VT_KERNEL_QUEUE;
+        vt_status s = VT_OK;
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+        for (int k = 0; k < kBatchChains && e == cudaSuccess; ++k) {
+            e = cudaStreamCreateWithFlags(&chain[k], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join[k], cudaEventDisableTiming);
         }
-        cudaStreamDestroy(cap);
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            if (queue) {
+                cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), cap);
+                k_render_batch<<<b->blocks, kBatchBlock, 0, cap>>>(b->d_jobs, b->njobs, b->total_units, b->d_counter);
+            } else {
+                // fork kBatchChains chains off the capture stream, jobs round robin, join
+                cudaEventRecord(fork, cap);
+                for (int k = 0; k < kBatchChains; ++k) cudaStreamWaitEvent(chain[k], fork, 0);
+                for (size_t j = 0; j < b->jobs.size() && !s; ++j) {
+                    const vt_job& jb = b->jobs[j];
+                    s = launch_render(ctx, jb.world, &jb.camera, &b->params, reinterpret_cast<uint4*>(jb.d_out),
+                                      chain[j % kBatchChains], false);
+                }
+                for (int k = 0; k < kBatchChains; ++k) {
+                    cudaEventRecord(join[k], chain[k]);
+                    cudaStreamWaitEvent(cap, join[k], 0);
+                }
+            }
+            const cudaError_t e2 = cudaStreamEndCapture(cap, &b->graph);
+            if (e == cudaSuccess) e = e2;
+        }
+        for (int k = 0; k < kBatchChains; ++k) {
+            if (chain[k]) cudaStreamDestroy(chain[k]);
+            if (join[k]) cudaEventDestroy(join[k]);
+        }
+        if (fork) cudaEventDestroy(fork);
+        if (cap) cudaStreamDestroy(cap);
+        if (s) return s;
         if (e != cudaSuccess) return check_cuda(ctx, e, "batch graph capture");
         VT_CUDA(ctx, cudaGraphInstantiate(&b->exec, b->graph, 0));
     }

@@ -233,7 +233,7 @@ class Context:
     def sync(self, stream=None) -> None:
         self.check(self.lib.vt_sync(self.handle, stream))
 
-    def set_tuning(self, kernel: int = KERNEL_TILE, warp_tile_w: int = 8, occupancy: int = 0,
+    def set_tuning(self, kernel: int = KERNEL_TILE, warp_tile_w: int = 8, occupancy: int = 1,
                    batch: int = 16) -> None:
         t = Tuning_t(kernel, warp_tile_w, occupancy, batch)
         self.check(self.lib.vt_set_tuning(self.handle, C.byref(t)))
