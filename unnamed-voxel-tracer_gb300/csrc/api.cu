@@ -26,6 +26,13 @@ vt_status check_cuda(vt_ctx* ctx, cudaError_t err, const char* what) {
     return fail(ctx, s, what, err);
 }
 
+vt_status take_status(vt_ctx* ctx, unsigned st) {
+    if (!st) return VT_OK;
+    VT_CUDA(ctx, cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
+    if (st & kStatusOob) return fail(ctx, VT_ERR_DEVICE_OOB, "a checked kernel saw an out-of-range index");
+    return fail(ctx, VT_ERR_TIMEOUT, "a bounded device wait gave up");
+}
+
 vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out) {
     if (bytes > ctx->scratch_bytes) {
         if (ctx->d_scratch) {
@@ -108,7 +115,7 @@ vt_status vt_ctx_destroy(vt_ctx* ctx) {
         }
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
-    if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
+    if (ctx->h_status) cudaFreeHost(ctx->h_status);
     for (int i = 0; i < kMaxBands; ++i)
         if (ctx->ev_band[i]) cudaEventDestroy(ctx->ev_band[i]);
     if (ctx->d_scratch) cudaFree(ctx->d_scratch);
@@ -127,12 +134,7 @@ vt_status vt_sync(vt_ctx* ctx, vt_stream stream) {
     VT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
     unsigned st = 0;
     VT_CUDA(ctx, cudaMemcpy(&st, ctx->d_status, sizeof(st), cudaMemcpyDeviceToHost));
-    if (st) {
-        VT_CUDA(ctx, cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
-        if (st & kStatusOob) return fail(ctx, VT_ERR_DEVICE_OOB, "a checked kernel saw an out-of-range index");
-        return fail(ctx, VT_ERR_TIMEOUT, "a bounded device wait gave up");
-    }
-    return VT_OK;
+    return take_status(ctx, st);
 }
 
 vt_status vt_device_info(vt_ctx* ctx, char* name, int32_t name_len, int32_t* sm_count) {

@@ -35,7 +35,10 @@ struct JobDesc {
 
 constexpr int kBatchBlock = 256;
 constexpr int kUnit = 16;  // pixels per unit side
-constexpr int kBatchChains = 8;
+#ifndef VT_BATCH_CHAINS
+#define VT_BATCH_CHAINS 8
+#endif
+constexpr int kBatchChains = VT_BATCH_CHAINS;
 
 __global__ void __launch_bounds__(kBatchBlock, 4) k_render_batch(const JobDesc* __restrict__ jobs, int njobs,
                                                                  unsigned total_units, unsigned* __restrict__ counter) {

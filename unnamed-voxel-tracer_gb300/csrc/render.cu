@@ -111,7 +111,7 @@ constexpr int kPersistBlock = 128;
 // vt_render_host splits frames of at least kPipelinePixels into
 // kPipelineBands row bands (at most kMaxBands).
 constexpr size_t kPipelinePixels = 1u << 18;
-constexpr int kPipelineBands = 8;
+constexpr int kPipelineBands = 16;
 static_assert(kPipelineBands <= kMaxBands, "band events");
 constexpr unsigned kGrab = 32;
 
@@ -300,7 +300,7 @@ vt_status band_streams(vt_ctx* ctx) {
     for (int i = 0; i < kBandStreams; ++i)
         VT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->band_stream[i], cudaStreamNonBlocking));
     VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_start, cudaEventDisableTiming));
-    VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming));
+    VT_CUDA(ctx, cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_status), sizeof(unsigned), cudaHostAllocDefault));
     for (int i = 0; i < kMaxBands; ++i) VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_band[i], cudaEventDisableTiming));
     VT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
     return VT_OK;
@@ -449,9 +449,11 @@ vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* ca
         VT_CUDA(ctx, cudaMemcpyAsync(h_out + (size_t)r0 * W, d_out + (size_t)r0 * W, (size_t)(r1 - r0) * W * sizeof(vt_hit),
                                      cudaMemcpyDeviceToHost, ctx->copy_stream));
     }
-    VT_CUDA(ctx, cudaEventRecord(ctx->ev_done, ctx->copy_stream));
-    VT_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_done, 0));
-    return vt_sync(ctx, ctx->stream);
+    // the status word rides on the copy stream: one synchronisation in all
+    VT_CUDA(ctx, cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                 ctx->copy_stream));
+    VT_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+    return take_status(ctx, *ctx->h_status);
 }
 
 vt_status vt_render_stats(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* params,

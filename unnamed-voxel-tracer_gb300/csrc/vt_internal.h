@@ -84,8 +84,9 @@ struct vt_ctx {
     // first use)
     cudaStream_t band_stream[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaStream_t copy_stream = nullptr;
-    cudaEvent_t ev_start = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_start = nullptr;
     cudaEvent_t ev_band[16] = {};
+    unsigned* h_status = nullptr;  // pinned copy of d_status
 };
 
 namespace vt {
@@ -145,6 +146,9 @@ namespace vt {
 // context and returns the matching status.
 vt_status fail(vt_ctx* ctx, vt_status s, const std::string& msg, cudaError_t err = cudaSuccess);
 vt_status check_cuda(vt_ctx* ctx, cudaError_t err, const char* what);
+// Turns a device status word read back by the caller into the call's status
+// (clearing the device word when it was set).
+vt_status take_status(vt_ctx* ctx, unsigned st);
 // Context-owned device buffer of at least `bytes` (grown on demand).
 vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out);
 // Rebuilds the empty-space distances of a world on `st`.
