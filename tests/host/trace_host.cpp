@@ -174,8 +174,9 @@ extern "C" int ht_trace_rays(const int32_t dims[3], const uint8_t* dense, const 
             hit = false;
             if (wk.start(w, r.o, r.d, max_steps)) {
                 int s;
+                const bool near = vt::near_origin(r.o);
                 do {
-                    s = wk.step<true>(w, w.cdist, h);
+                    s = near ? wk.step<true, true, true>(w, w.cdist, h) : wk.step<true, true, false>(w, w.cdist, h);
                     counters[0]++;
                 } while (s == vt::Walker::kMore);
                 hit = s == vt::Walker::kHit;

@@ -97,6 +97,28 @@ def test_sparse_world_long_rays(ht, oracle):
     check(ht, oracle, mats, o, d, 1 << 20)
 
 
+def test_far_origins_and_unnormalised_directions(ht, oracle, vtlib):
+    """Origins up to ~4e6 away (both sides of the 2^20 bound below which the
+    jump's plane search takes a single correction) aimed at the world, with
+    direction lengths from 1e-3 to 1e3."""
+    dims = (96, 64, 80)
+    d = vtlib.gen_desc(dims, scale=0.5, seed=9, trees=15, caves=True)
+    mats = vtlib.gen_world(d)
+    rng = np.random.default_rng(9)
+    n = 6000
+    target = rng.uniform([0, 0, 0], dims, (n, 3))
+    away = rng.normal(size=(n, 3))
+    away /= np.linalg.norm(away, axis=1, keepdims=True)
+    dist = 10.0 ** rng.uniform(1, 6.6, n)
+    o = target + away * dist[:, None]
+    dirs = (target - o) / dist[:, None] * (10.0 ** rng.uniform(-3, 3, n))[:, None]
+    o, dirs = np.ascontiguousarray(o, np.float32), np.ascontiguousarray(dirs, np.float32)
+    assert (np.abs(o).max(axis=1) >= 2 ** 20).sum() > 300 and (np.abs(o).max(axis=1) < 2 ** 20).sum() > 3000
+    check(ht, oracle, mats, o, dirs, 1 << 24)
+    got, _ = run_host(ht, mats, o, dirs, 1 << 24, 1)
+    assert (got["face"] != 0xFF).sum() > 1500
+
+
 def test_counters_match_oracle(ht, oracle, vtlib):
     d = vtlib.gen_desc((128, 64, 96), scale=0.5, seed=4, trees=5)
     mats = vtlib.gen_world(d)

@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_shade(AdjArgs a) {
                 PRay rs;
                 pray_init(rs, so, a.sun);
                 TraceHit hs;
-                lit = !trace_fast<false>(a.w, cd, rs, a.shadow_steps, hs) &&
+                lit = !trace_fast<false, true, true>(a.w, cd, rs, a.shadow_steps, hs) &&
                       !(a.w.n_entities > 0 && entity_occluded(a.w, so, a.sun));
             }
             ndl_raw = dot3(nrm, a.sun_n);

@@ -84,7 +84,8 @@ __global__ void __launch_bounds__(kBlock) k_trace_rays(WorldView w, const float*
     pray_init(r, o, d);
     TraceHit h;
     TraceCounters cnt;
-    const bool hit = trace_fast<true, true>(w, w.cdist, r, max_steps, h);
+    const bool hit = near_origin(r.o) ? trace_fast<true, true, true>(w, w.cdist, r, max_steps, h)
+                                      : trace_fast<true, true, false>(w, w.cdist, r, max_steps, h);
     if (hit) {
         const int e = h.axis;
         const bool pe = e == 0 ? r.pos[0] : (e == 1 ? r.pos[1] : r.pos[2]);

@@ -15,12 +15,15 @@ struct PixelCounters {
 // The instrumented and bounds-checked variants run the three-level model
 // traversal (it defines the algorithmic byte counts); the production variant
 // runs trace_fast.  Both give identical results.
-template <bool STATS, bool CHECKED, bool MAT, bool RUN, class Coarse>
+// NEAR: the caller knows the origin passes near_origin (secondary rays start
+// on a hit inside the grid); otherwise the primary ray checks it once.
+template <bool STATS, bool CHECKED, bool MAT, bool NEAR, class Coarse>
 __device__ __forceinline__ bool trace_any(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
                                           const PRay& r, int max_steps, TraceHit& h, TraceCounters& cnt,
                                           unsigned* status) {
     if (STATS || CHECKED) return trace_p<STATS, CHECKED, MAT>(w, coarse, r, max_steps, h, cnt, status);
-    return trace_fast<MAT, RUN>(w, cd, r, max_steps, h);
+    if (NEAR || near_origin(r.o)) return trace_fast<MAT, true, true>(w, cd, r, max_steps, h);
+    return trace_fast<MAT, true, false>(w, cd, r, max_steps, h);
 }
 
 template <bool STATS, bool CHECKED, class Coarse>
@@ -33,7 +36,7 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
     pray_init(r, o, d);
     TraceHit h;
     TraceCounters cnt;
-    const bool hit = trace_any<STATS, CHECKED, true, true>(w, coarse, cd, r, f.max_steps, h, cnt, status);
+    const bool hit = trace_any<STATS, CHECKED, true, false>(w, coarse, cd, r, f.max_steps, h, cnt, status);
     if (STATS) {
         pc.v[0] += 1;
         pc.v[9] += 16;

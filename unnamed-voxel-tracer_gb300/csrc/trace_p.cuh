@@ -46,6 +46,12 @@ __device__ __forceinline__ void pray_init(PRay& r, const float o[3], const float
     }
 }
 
+// Whether a ray origin is near enough for the one-correction plane search
+// (advance_axis<true>).
+__host__ __device__ __forceinline__ bool near_origin(const float o[3]) {
+    return fabsf(o[0]) < 0x1p20f && fabsf(o[1]) < 0x1p20f && fabsf(o[2]) < 0x1p20f;
+}
+
 __device__ __forceinline__ float ptime(const PRay& r, int i, int k) {
     return __fmaf_rn(__int2float_rn(k), r.inv[i], r.oinv[i]);
 }
@@ -62,10 +68,32 @@ __device__ __forceinline__ bool crossed(const PRay& r, int i, int k, float T, in
 // Cell of axis i at the event (T, e), i != e.  Positive direction: the largest
 // k in [lo, K-1] whose plane k is crossed (lo if none); negative direction: the
 // smallest k in [K, lo] whose plane k+1 is crossed (lo if none).  A rounded
-// position gives the first guess; the exact plane times decide.
+// position p = o + d T gives the first guess g = floor(p); the exact plane
+// times decide.
+//
+// When |o_i| < 2^20 and the cells lie in the grid (< 2^13), the guess is off
+// by at most one plane: the rounding of p and of the plane times ptime(k) =
+// fma(k, 1/d, -o/d) stays below 2^-24 * 2^21 = 1/8 of a cell in position, so
+// plane g - 1 is crossed strictly before T and plane g + 2 strictly after, and
+// one exact test up or down settles it (NEAR).  Otherwise (far origins) the
+// walk corrects the guess plane by plane.
+template <bool NEAR>
 __device__ __forceinline__ int advance_axis(const PRay& r, int i, int lo, int K, float T, int e) {
     float p = __fmaf_rn(r.d[i], T, r.o[i]);
     int k = __float2int_rd(p);
+    if (NEAR) {
+        if (r.pos[i]) {
+            const int hi = K - 1;
+            k = min(max(k, lo), hi);
+            if (k < hi && crossed(r, i, k + 1, T, e)) ++k;
+            else if (k > lo && !crossed(r, i, k, T, e)) --k;
+        } else {
+            k = min(max(k, K), lo);
+            if (k > K && crossed(r, i, k, T, e)) --k;
+            else if (k < lo && !crossed(r, i, k + 1, T, e)) ++k;
+        }
+        return k;
+    }
     if (r.pos[i]) {
         int hi = K - 1;
         k = min(max(k, lo), hi);
@@ -101,7 +129,7 @@ __device__ __forceinline__ bool pray_start(const PRay& r, const int D[3], int c[
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             if (i == e) c[i] = r.pos[i] ? 0 : D[i] - 1;
-            else c[i] = r.pos[i] ? advance_axis(r, i, 0, D[i], T0, e) : advance_axis(r, i, D[i] - 1, 0, T0, e);
+            else c[i] = r.pos[i] ? advance_axis<false>(r, i, 0, D[i], T0, e) : advance_axis<false>(r, i, D[i] - 1, 0, T0, e);
         }
         t0 = T0;
         axis0 = e;
@@ -246,7 +274,7 @@ __device__ __forceinline__ bool trace_p(const WorldView& w, const Coarse& coarse
                     c[i] = cn;
                     tm[i] = ptime(r, i, r.pos[i] ? cn + 1 : cn);
                 } else if (key_lt(tm[i], i, T, e)) {
-                    const int cn = advance_axis(r, i, c[i], K[i], T, e);
+                    const int cn = advance_axis<false>(r, i, c[i], K[i], T, e);
                     crossings += abs(cn - c[i]);
                     c[i] = cn;
                     tm[i] = ptime(r, i, r.pos[i] ? cn + 1 : cn);
@@ -328,7 +356,8 @@ struct Walker {
     // jump and the unit-step code; running a lane's unit steps in one inner
     // loop pays the jump code once per brick visit instead (-4.5% on a 1080p
     // terrain frame of primary and shadow rays).
-    template <bool MAT, bool RUN = true>
+    // NEAR: the ray's origin passes near_origin (one-correction plane search).
+    template <bool MAT, bool RUN = true, bool NEAR = false>
     __device__ __forceinline__ int step(const WorldView& w, const unsigned char* cdist, TraceHit& h) {
         bool jump = false;
         int sh = 0, rad = 0;
@@ -425,7 +454,7 @@ struct Walker {
         for (int i = 0; i < 3; ++i) {
             int cn = c[i];
             if (i == e) cn = r.pos[i] ? K[i] : K[i] - 1;
-            else if (key_lt(tm[i], i, T, e)) cn = advance_axis(r, i, c[i], K[i], T, e);
+            else if (key_lt(tm[i], i, T, e)) cn = advance_axis<NEAR>(r, i, c[i], K[i], T, e);
             crossings += abs(cn - c[i]);
             c[i] = cn;
             nk[i] = r.pos[i] ? cn + 1 : cn;
@@ -443,13 +472,13 @@ struct Walker {
     }
 };
 
-template <bool MAT, bool RUN = true>
+template <bool MAT, bool RUN = true, bool NEAR = false>
 __device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned char* cdist, const PRay& r,
                                            int max_steps, TraceHit& h) {
     Walker wk;
     if (!wk.start(w, r.o, r.d, max_steps)) return false;
     int s;
-    while ((s = wk.step<MAT, RUN>(w, cdist, h)) == Walker::kMore) {
+    while ((s = wk.step<MAT, RUN, NEAR>(w, cdist, h)) == Walker::kMore) {
     }
     return s == Walker::kHit;
 }
