@@ -460,7 +460,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                                                                        "coarse_words")},
         "e2e": {"value": e2e_value, "unit": "Grays/s", "h2d_bytes_per_step": C.sizeof(vt.Camera_t) + C.sizeof(vt.Params_t),
                 "d2h_bytes_per_step": nbytes,
-                "note": "vt_render_host: camera and params travel in the launch; records copied to pinned host memory"},
+                "note": "vt_render_host into pinned host memory: camera and params travel in the launch; the kernel writes the records across the host link"},
         "cpu_baseline": cpu, "clocks": clk.summary(), "device": {"name": name, "sms": sms},
         **extra,
     }

@@ -205,7 +205,10 @@ void vt_params_default(vt_params* p);
  * v = -1 (bottom of the image, as the GL image is addressed). */
 vt_status vt_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
                     const vt_params* params, vt_hit* d_out, vt_stream stream);
-/* Same, with host output: copies the records back and synchronises. */
+/* Same, with host output, synchronous.  Into pinned memory (vt_host_alloc_
+ * pinned) the kernel writes the records directly over the host link; into
+ * pageable memory frames of >= 2^18 pixels render as 16 row bands on four
+ * streams, each band copied back as soon as it is done. */
 vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
                          const vt_params* params, vt_hit* h_out);
 

@@ -137,8 +137,9 @@ def test_repeated_frames_are_identical(vt, tuned):
 @pytest.mark.parametrize("tw", [8, 16, 32])
 def test_render_host_pipeline_equals_device_render(vt, tuned, tw):
     """Frames of >= 2^18 pixels go through vt_render_host's row-band pipeline
-    (bands on several streams, each copied out when done); the records equal
-    one device-side vt_render of the frame."""
+    (bands on several streams, each copied out when done) into pageable
+    memory, and are written by the kernel itself into pinned memory; both
+    equal one device-side vt_render of the frame."""
     d = vt.gen_desc((256, 128, 256), seed=6, trees=40)
     w = make_world(vt, tuned, vt.gen_world(d))
     tuned.set_tuning(kernel=0, warp_tile_w=tw, occupancy=1)
@@ -154,6 +155,14 @@ def test_render_host_pipeline_equals_device_render(vt, tuned, tw):
             got = vt.render_host(tuned, w, cam, p)
             assert np.array_equal(got, want), (W, H)
             assert (got["face"] != 0xFF).sum() > 1000
+            # pinned memory: the kernel writes the records straight into it
+            pb = vt.PinnedBuffer(tuned, W * H, vt.HIT_DTYPE)
+            try:
+                pb.array[:] = np.zeros(1, vt.HIT_DTYPE)
+                vt.render_host(tuned, w, cam, p, pb.array)
+                assert np.array_equal(pb.array, want), (W, H)
+            finally:
+                pb.free()
     finally:
         w.close()
 

@@ -295,6 +295,24 @@ class DeviceBuffer:
             self.ptr = None
 
 
+class PinnedBuffer:
+    """Page-locked host memory (vt_host_alloc_pinned) seen as a numpy array."""
+
+    def __init__(self, ctx: Context, count: int, dtype):
+        self.ctx, dtype = ctx, np.dtype(dtype)
+        p = C.c_void_p()
+        ctx.check(ctx.lib.vt_host_alloc_pinned(ctx.handle, max(1, count * dtype.itemsize), C.byref(p)))
+        self.ptr = p.value
+        raw = (C.c_uint8 * (count * dtype.itemsize)).from_address(self.ptr)
+        self.array = np.frombuffer(raw, dtype=dtype, count=count)
+
+    def free(self) -> None:
+        if self.ptr:
+            self.array = None
+            self.ctx.lib.vt_host_free_pinned(self.ctx.handle, self.ptr)
+            self.ptr = None
+
+
 # -------------------------------------------------------------------- world
 class World:
     """Mode-P voxel world on the device (VoxelBrickmap, voxel.zig:25-82)."""
