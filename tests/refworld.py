@@ -1,4 +1,6 @@
-"""Worlds in the reference's own format, for the mode-R oracle checks.
+"""Worlds in the reference's own format, for the mode-R oracle checks (the
+builders live in the package, unnamed-voxel-tracer_gb300/brickmap.py; the
+.vox writer/reader and the ray sampler are test helpers).
 
 The reference stores a 512^3 voxel map as a 64^3 table of brick indices
 (0 = empty, else brick + 1; index x + 64*(y + 64*z), voxel.zig:21-23) and a
@@ -12,44 +14,7 @@ from __future__ import annotations
 import numpy as np
 
 
-def random_models(rng: np.random.Generator, n: int, full: bool = False) -> list[np.ndarray]:
-    """n models, each an (8, 8, 8) [z, y, x] array of RGBA8 texels (0 = empty)."""
-    out = []
-    for i in range(n):
-        density = 1.0 if full else rng.uniform(0.2, 1.0)
-        keep = rng.random((8, 8, 8)) < density
-        rgb = rng.integers(1, 256, size=(8, 8, 8, 3), dtype=np.uint32)
-        tex = rgb[..., 0] | (rgb[..., 1] << 8) | (rgb[..., 2] << 16) | (np.uint32(255) << 24)
-        out.append(np.where(keep, tex, 0).astype(np.uint32))
-    return out
-
-
-def build_atlas(models: list[np.ndarray]) -> np.ndarray:
-    atlas = np.zeros((256, 256, 256), dtype=np.uint32)  # [z, y, x]
-    for s, m in enumerate(models):
-        ox, oy, oz = (s & 31) * 8, ((s >> 5) & 31) * 8, ((s >> 10) & 31) * 8
-        atlas[oz:oz + 8, oy:oy + 8, ox:ox + 8] = m
-    return atlas.reshape(-1)
-
-
-def build_map(mats: np.ndarray, model_of_material: np.ndarray):
-    """Dense uint8 materials [z, y, x] (at most 512 per axis) -> (chunks, data).
-    Material m != 0 becomes the solid voxel of model model_of_material[m]."""
-    Z, Y, X = mats.shape
-    assert max(X, Y, Z) <= 512
-    cz, cy, cx = (Z + 7) // 8, (Y + 7) // 8, (X + 7) // 8
-    grid = np.zeros((cz * 8, cy * 8, cx * 8), dtype=np.uint8)
-    grid[:Z, :Y, :X] = mats
-    words = np.where(grid != 0, (model_of_material[grid].astype(np.uint32) & 0xFFFFFFF) | (1 << 28), 0)
-    bricks = words.astype(np.uint32).reshape(cz, 8, cy, 8, cx, 8)   # [bz, z, by, y, bx, x]
-    occupied = np.zeros((64, 64, 64), dtype=bool)                   # [bz, by, bx]
-    occupied[:cz, :cy, :cx] = (bricks != 0).any(axis=(1, 3, 5))
-    chunks = np.zeros((64, 64, 64), dtype=np.uint32)
-    idx = np.flatnonzero(occupied.reshape(-1))                      # chunk index x + 64*(y + 64*z)
-    chunks.reshape(-1)[idx] = np.arange(1, idx.size + 1, dtype=np.uint32)
-    bz, by, bx = np.unravel_index(idx, (64, 64, 64))
-    data = bricks[bz, :, by, :, bx, :]                              # [k, z, y, x]
-    return chunks.reshape(-1), np.ascontiguousarray(data.reshape(-1)).astype(np.uint32)
+from brickmap import build_atlas, build_map, random_models  # noqa: E402,F401  (the package's builders)
 
 
 def random_rays(rng: np.random.Generator, lo, hi, n: int):

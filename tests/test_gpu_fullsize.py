@@ -1,0 +1,102 @@
+"""Parity at the benchmark's full sizes.
+
+  - the 512x256x512 world (200 trees) at 1920x1080, primary + shadow rays,
+    all 8 benchmark cameras, every pixel against the oracle;
+  - the 2048x256x2048 world with caves (1 GiB of materials) at 3840x2160,
+    primary + shadow + bounce rays, every 16th row against the oracle;
+  - size-independent properties of the full frames: the records of the
+    batched graph and of the pinned-memory path equal vt_render's, and the
+    instrumented kernel's counters equal the oracle's on sampled rows.
+
+The oracle runs multithreaded on the host (about a second per 1080p frame on
+16 cores)."""
+import os
+
+import numpy as np
+import pytest
+
+from test_gpu_render import compare
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 4
+
+
+@pytest.fixture(scope="module")
+def world1(vt, ctx, oracle):
+    d = vt.gen_desc((512, 256, 512), seed=1, trees=200)
+    mats = vt.gen_world(d)
+    w = vt.World(ctx, (512, 256, 512))
+    w.upload_dense(mats)
+    yield d, mats, w, oracle.OracleWorld(mats)
+    w.close()
+
+
+def test_benchmark_frames_match_oracle(vt, ctx, oracle, world1):
+    d, mats, w, ow = world1
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, max_steps=512, shadow_max_steps=512,
+                          sun_dir=vt.gen_sun(1))
+    hits = 0
+    for cs in range(8):
+        cam = vt.gen_camera(d, cs, 1920, 1080)
+        gpu = vt.render_host(ctx, w, cam, p)
+        ref, _ = oracle.render(ow, vt.default_palette(), cam, p, threads=THREADS)
+        compare(gpu, ref)
+        hits += int((gpu["flags"] & vt.HIT_PRIMARY).sum())
+    assert hits > 8 * 1920 * 1080 // 3
+
+
+def test_benchmark_frame_paths_agree(vt, ctx, world1):
+    """vt_render (device), vt_render_host into pinned memory and a batch of
+    the 8 cameras give the same records."""
+    d, mats, w, _ = world1
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=vt.gen_sun(1))
+    cams = [vt.gen_camera(d, cs, 1920, 1080) for cs in range(8)]
+    bufs = [ctx.alloc(1920 * 1080 * 16) for _ in cams]
+    pb = vt.PinnedBuffer(ctx, 1920 * 1080, vt.HIT_DTYPE)
+    try:
+        batch = vt.Batch(ctx, [(w, c, b) for c, b in zip(cams, bufs)], p)
+        batch.launch()
+        ctx.sync()
+        for c, b in zip(cams, bufs):
+            want = b.download(np.zeros(1920 * 1080, vt.HIT_DTYPE))
+            vt.render_host(ctx, w, c, p, pb.array)
+            assert np.array_equal(pb.array, want)
+        batch.close()
+    finally:
+        pb.free()
+        for b in bufs:
+            b.free()
+
+
+def test_counters_match_oracle_full_frame(vt, ctx, oracle, world1):
+    d, mats, w, ow = world1
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=vt.gen_sun(1))
+    cam = vt.gen_camera(d, 5, 1920, 1080)
+    st = vt.render_stats(ctx, w, cam, p)
+    _, ref = oracle.render(ow, vt.default_palette(), cam, p, threads=THREADS)
+    for k in ("primary_rays", "primary_hits", "shadow_rays", "shadow_hits", "mask_words", "coarse_words",
+              "material_bytes", "record_bytes", "steps"):
+        assert st[k] == ref[k], k
+
+
+def test_config2_world_4k_with_bounce_rays_sampled_rows(vt, ctx, oracle):
+    import scenes
+    desc, cams, params = scenes.config2()
+    X, Y, Z = desc.dims
+    w = vt.World(ctx, (X, Y, Z))
+    try:
+        w.generate(desc)                      # on the device, same bytes as the host generator
+        mats = w.download_dense()
+        ow = oracle.OracleWorld(mats)
+        cam = cams[0]
+        gpu = vt.render_host(ctx, w, cam, params)
+        step = 16
+        ref, st = oracle.render(ow, vt.default_palette(), cam, params, threads=THREADS, row_step=step)
+        rows = np.arange(0, cam.height, step)
+        g = gpu.reshape(cam.height, cam.width)[rows].reshape(-1)
+        r = ref.reshape(cam.height, cam.width)[rows].reshape(-1)
+        compare(g, r)
+        assert st["bounce_rays"] > 100000 and st["bounce_hits"] > 1000
+    finally:
+        w.close()
