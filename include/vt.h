@@ -301,6 +301,18 @@ vt_status vt_trace_map(vt_ctx* ctx, const vt_brickmap* bm, const float* d_origin
  * vt_ref_pixel records on the device.  Rows are the GL image's rows. */
 vt_status vt_render_reference(vt_ctx* ctx, const vt_brickmap* bm, const vt_camera* cam, vt_ref_pixel* d_out,
                               vt_stream stream);
+/* procgen (src/procgen.zig:6-70) into the reference's world format: the
+ * stone floor, the heightfield columns, grass, flowers and trees, every
+ * choice drawn from util.LCG (seed 0x46AE4F, util.zig:33-45) in the
+ * reference's order, bricks allocated in order of first touch as
+ * VoxelBrickmap(dim, 8).set does (voxel.zig:47-61).  h_chunks receives the
+ * (dim/8)^3 table, h_bricks up to brick_capacity bricks of 512 u32, *nbricks
+ * the count used (VT_ERR_OOM when it exceeds the capacity: call again with
+ * more).  The heightfield noise (FastNoiseLite fbm in the reference, not part
+ * of its sources) comes from h_noise[x*dim + z] when given, else from the
+ * library's seeded value-noise fbm at ((offset + x)/10, (offset + z)/10). */
+vt_status vt_procgen_reference(int32_t dim, float offset_x, float offset_z, const float* h_noise, uint64_t noise_seed,
+                               uint32_t* h_chunks, uint32_t* h_bricks, size_t brick_capacity, size_t* nbricks);
 /* VoxelBrickmap.get over the whole map (voxel.zig:63-70): the chunk table
  * (64^3 u32) and the first nbricks bricks (512 u32 each) back to the host,
  * after all work queued on the device. */

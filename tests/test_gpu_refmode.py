@@ -81,3 +81,27 @@ def test_load_vox_equals_decoded_models(vt, ctx, refscene):
     finally:
         a.close()
         b.close()
+
+
+def test_reference_procgen_world_frame(vt, ctx, oracle):
+    """The reference's own generator (vt_procgen_reference, 512^3, seeded
+    noise) uploaded as a brickmap and rendered: the GPU frame equals the
+    oracle's."""
+    chunks, bricks = vt.procgen_reference(512, None, seed=11)
+    rng = np.random.default_rng(11)
+    atlas = refworld.build_atlas(refworld.random_models(rng, 29))
+    bm = vt.Brickmap(ctx)
+    try:
+        bm.upload(chunks, bricks)
+        bm.set_atlas(atlas, 29)
+        ow = oracle.OracleRefWorld(chunks, bricks, atlas)
+        for yaw in (0.7, 2.5):
+            cam = vt.Camera(pos=(200.0, 70.0, 180.0), yaw=yaw, pitch=-0.45, fov=1.2, width=96, height=72)
+            c = cam.as_uniform_data()
+            got, want = bm.render(c), oracle.render_reference(ow, c)
+            for f in ("normal", "illumination"):
+                assert np.array_equal(got[f], want[f]), f
+            assert np.array_equal(got["position"].view(np.uint32), want["position"].view(np.uint32))
+            assert (got["position"][:, 0] >= 0).sum() > 1000
+    finally:
+        bm.close()

@@ -28,6 +28,7 @@ LIB_PATH = _HERE / "lib" / "libvt.so"
 
 # ---------------------------------------------------------------- constants
 VT_OK = 0
+VT_ERR_OOM = 2
 STATUS_NAMES = {0: "VT_OK", 1: "VT_ERR_ARG", 2: "VT_ERR_OOM", 3: "VT_ERR_CUDA", 4: "VT_ERR_DEVICE_OOB",
                 5: "VT_ERR_TIMEOUT", 6: "VT_ERR_NO_DEVICE", 7: "VT_ERR_FORMAT", 8: "VT_ERR_STATE"}
 RAYS_PRIMARY, RAYS_SHADOW, RAYS_BOUNCE = 1, 2, 4
@@ -160,6 +161,8 @@ _SIGNATURES = {
     "vt_gen_desc_init": (None, [C.POINTER(GenDesc_t), C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64]),
     "vt_gen_world": (_S, [C.POINTER(GenDesc_t), _P, C.c_size_t, C.c_int32]),
     "vt_gen_height": (C.c_int32, [C.POINTER(GenDesc_t), C.c_int32, C.c_int32]),
+    "vt_procgen_reference": (_S, [C.c_int32, C.c_float, C.c_float, _P, C.c_uint64, _P, _P, C.c_size_t,
+                                  C.POINTER(C.c_size_t)]),
     "vt_world_generate": (_S, [_P, C.POINTER(GenDesc_t), _P]),
     "vt_gen_camera": (_S, [C.POINTER(GenDesc_t), C.c_uint64, C.c_int32, C.c_int32, C.POINTER(Camera_t)]),
     "vt_default_palette": (_S, [_P]),
@@ -704,6 +707,26 @@ def gen_world(desc: GenDesc_t, threads: int = 0) -> np.ndarray:
     out = np.zeros((Z, Y, X), dtype=np.uint8)
     _check(load().vt_gen_world(C.byref(desc), _ptr(out), out.nbytes, threads))
     return out
+
+
+def procgen_reference(dim: int = 512, noise: np.ndarray | None = None, seed: int = 0, offset=(0.0, 0.0)):
+    """The reference's procgen (procgen.zig:6-70) in its own world format:
+    (chunks [(dim/8)^3] u32, bricks [n*512] u32).  noise: (dim, dim) heightfield
+    noise indexed [x, z] (FastNoiseLite's role), or None for the seeded fbm."""
+    cd = dim // 8
+    chunks = np.zeros(cd ** 3, np.uint32)
+    nz = None if noise is None else np.ascontiguousarray(noise, np.float32).reshape(dim * dim)
+    cap = cd * cd * 4
+    while True:
+        bricks = np.zeros(cap * 512, np.uint32)
+        n = C.c_size_t()
+        st = load().vt_procgen_reference(dim, float(offset[0]), float(offset[1]), _ptr(nz) if nz is not None else None,
+                                         int(seed), _ptr(chunks), _ptr(bricks), cap, C.byref(n))
+        if st == VT_OK:
+            return chunks, bricks[:n.value * 512].copy()
+        if st != VT_ERR_OOM:
+            _check(st)
+        cap = max(cap * 2, n.value)
 
 
 def gen_camera(desc: GenDesc_t, seed: int, width: int, height: int) -> Camera_t:
