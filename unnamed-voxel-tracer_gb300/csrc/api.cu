@@ -92,6 +92,8 @@ vt_status vt_ctx_create(int32_t device, vt_ctx** out) {
         if ((e = cudaMemset(ctx->d_status, 0, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMemset"); break; }
         if ((e = cudaMalloc(&ctx->d_counters, kNumCounters * sizeof(unsigned long long))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
         if ((e = cudaMalloc(&ctx->d_work, kWorkSlots * sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
+        if ((e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_status), sizeof(unsigned), cudaHostAllocDefault)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaHostAlloc"); break; }
+        *ctx->h_status = 0;
         // blocking stream: *_host calls order after work queued on the legacy default stream
         if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamDefault)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaStreamCreate"); break; }
     } while (0);
@@ -131,10 +133,11 @@ const char* vt_last_error_string(const vt_ctx* ctx) { return ctx ? ctx->last_err
 
 vt_status vt_sync(vt_ctx* ctx, vt_stream stream) {
     if (!ctx) return VT_ERR_ARG;
+    // the status word travels on the same stream: one synchronisation
+    VT_CUDA(ctx, cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                 (cudaStream_t)stream));
     VT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
-    unsigned st = 0;
-    VT_CUDA(ctx, cudaMemcpy(&st, ctx->d_status, sizeof(st), cudaMemcpyDeviceToHost));
-    return take_status(ctx, st);
+    return take_status(ctx, *ctx->h_status);
 }
 
 vt_status vt_device_info(vt_ctx* ctx, char* name, int32_t name_len, int32_t* sm_count) {

@@ -301,7 +301,6 @@ vt_status band_streams(vt_ctx* ctx) {
     for (int i = 0; i < kBandStreams; ++i)
         VT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->band_stream[i], cudaStreamNonBlocking));
     VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_start, cudaEventDisableTiming));
-    VT_CUDA(ctx, cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_status), sizeof(unsigned), cudaHostAllocDefault));
     for (int i = 0; i < kMaxBands; ++i) VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_band[i], cudaEventDisableTiming));
     VT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
     return VT_OK;
