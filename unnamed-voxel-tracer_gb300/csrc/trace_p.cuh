@@ -308,7 +308,7 @@ __device__ __forceinline__ bool trace_p(const WorldView& w, const Coarse& coarse
 //     voxel's bit index moves by +-1, 4 or 16.
 // The walk is resumable one iteration at a time (step), so that a persistent
 // kernel can interleave rays of different pixels and kinds in one warp.
-// cdist is the per-chunk distance array (in shared memory in the kernels).
+// cdist is the per-chunk distance array (8 octant fields, read through L1).
 // Host builds of this header (the traversal tests) may count the kinds of
 // steps (0 chunk jump, 1 brick jump, 2 voxel test + unit step).
 #ifndef VT_STEP_HOOK
