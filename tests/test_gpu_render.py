@@ -81,6 +81,41 @@ def test_trace_rays_kat(vt, oracle, ctx):
     w.close()
 
 
+def test_far_origins_both_walker_variants(vt, oracle, ctx):
+    """Origins on both sides of |o| = 2^20 (the walker's one-correction plane
+    search below it, the correction loop above), aimed at the world, with
+    direction lengths from 1e-3 to 1e3; then a frame from a camera 3e6 voxels
+    away, whose primary rays take the far variant."""
+    dims = (96, 64, 80)
+    d = vt.gen_desc(dims, scale=0.5, seed=9, trees=15, caves=True)
+    mats = vt.gen_world(d)
+    w = make_world(vt, ctx, mats)
+    rng = np.random.default_rng(9)
+    n = 20000
+    target = rng.uniform([0, 0, 0], dims, (n, 3))
+    away = rng.normal(size=(n, 3))
+    away /= np.linalg.norm(away, axis=1, keepdims=True)
+    dist = 10.0 ** rng.uniform(1, 6.6, n)
+    o = (target + away * dist[:, None]).astype(np.float32)
+    dirs = ((target - o) / dist[:, None] * (10.0 ** rng.uniform(-3, 3, n))[:, None]).astype(np.float32)
+    far = np.abs(o).max(axis=1) >= 2 ** 20
+    assert far.sum() > 1000 and (~far).sum() > 10000
+    gpu = vt.trace_rays(ctx, w, o, dirs, 1 << 24)
+    compare(gpu, oracle.trace_rays(oracle.OracleWorld(mats), o, dirs, 1 << 24), rgb_tol=0)
+    assert (gpu["face"][far] != 0xFF).sum() > 300
+    pos = np.array([3.0e6, 3.0e4, 2.5e6])
+    to = np.array(dims, float) / 2 - pos
+    cam = vt.Camera(pos=tuple(pos), yaw=float(np.arctan2(to[0], to[2])),
+                    pitch=float(np.arcsin(to[1] / np.linalg.norm(to))), fov=4e-5, width=96, height=64)
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, max_steps=1 << 26, sun_dir=vt.gen_sun(9))
+    c = cam.as_uniform_data()
+    gpu = vt.render_host(ctx, w, c, p)
+    ref, _ = oracle.render(oracle.OracleWorld(mats), vt.default_palette(), c, p, threads=8)
+    compare(gpu, ref)
+    assert (gpu["face"] != 0xFF).sum() > 500
+    w.close()
+
+
 @pytest.mark.parametrize("shade", ["none", "reference"])
 def test_config0_frame(vt, oracle, ctx, shade):
     """128^3 terrain, 640x360, primary rays, max 512 steps."""
