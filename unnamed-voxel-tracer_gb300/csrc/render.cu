@@ -122,6 +122,10 @@ __device__ __forceinline__ void pixel_of(unsigned idx, unsigned tiles_x, int& px
     py = (int)((tile / tiles_x) * 4u + (l >> 3));
 }
 
+// NEAR: the camera passes near_origin, so every ray of the frame does
+// (secondary rays start inside the grid) and the walk takes the
+// one-correction plane search.
+template <bool NEAR>
 __global__ void __launch_bounds__(kPersistBlock) k_render_persist(WorldView w, FrameParams f, uint4* __restrict__ out,
                                                                   unsigned* __restrict__ work, unsigned total,
                                                                   unsigned tiles_x, int batch) {
@@ -143,7 +147,7 @@ __global__ void __launch_bounds__(kPersistBlock) k_render_persist(WorldView w, F
     for (;;) {
         if (active) {
             TraceHit h;
-            const int s = wk.step<true>(w, cd, h);
+            const int s = wk.step<true, true, NEAR>(w, cd, h);
             if (s != Walker::kMore) {
                 active = false;
                 res = s;
@@ -328,7 +332,7 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         // of the context's ring, zeroed on this stream before the launch
         if (ctx->persist_blocks == 0) {
             int nb = 0;
-            VT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_render_persist, kPersistBlock, 0));
+            VT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_render_persist<true>, kPersistBlock, 0));
             ctx->persist_blocks = nb > 0 ? nb : 1;
         }
         unsigned* counter = ctx->d_work + (ctx->work_slot++ % kWorkSlots);
@@ -337,7 +341,10 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         const unsigned total = tiles_x * tiles_y * 32u;
         const unsigned blocks = (unsigned)(ctx->sm_count * ctx->persist_blocks);
         const int batch = tu.batch;
-        k_render_persist<<<blocks, kPersistBlock, 0, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
+        if (near_origin(f.pos))
+            k_render_persist<true><<<blocks, kPersistBlock, 0, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
+        else
+            k_render_persist<false><<<blocks, kPersistBlock, 0, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
         VT_CUDA(ctx, cudaGetLastError());
         return VT_OK;
     }
