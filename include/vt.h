@@ -393,7 +393,7 @@ vt_status vt_shade_backward(vt_ctx* ctx, const vt_world* world, const vt_camera*
 typedef struct {
     int32_t kernel;       /* VT_KERNEL_* */
     int32_t warp_tile_w;  /* VT_KERNEL_TILE: a warp's tile is w x (32/w) pixels, w in {8, 16, 32} */
-    int32_t occupancy;    /* VT_KERNEL_TILE: 1 = register budget capped for 40 warps per SM */
+    int32_t occupancy;    /* VT_KERNEL_TILE: 1 = register budget capped for 4 blocks (32 warps) per SM */
     int32_t batch;        /* VT_KERNEL_QUEUE: parked lanes (1..32) that trigger a refill pass */
 } vt_tuning;
 vt_status vt_set_tuning(vt_ctx* ctx, const vt_tuning* tuning);

@@ -31,7 +31,10 @@ __device__ __forceinline__ void flush_counters(PixelCounters& pc, unsigned long 
 
 // One thread per pixel.  A warp covers a TW x (32 / TW) pixel tile; the
 // 256-thread block covers max(16, TW) pixels across.  OCC caps the register
-// budget so that 5 blocks (40 warps) fit on an SM.
+// budget so that kOccBlocks blocks fit on an SM: 4 blocks (64 registers, 32
+// warps, no spills) measured 4% faster on a 1080p frame than 5 (48 registers
+// with spills) and 3 (uncapped, 67 registers).
+constexpr int kOccBlocks = 4;
 template <int TW>
 struct BlockTile {
     static constexpr int kW = TW < 16 ? 16 : TW;     // block tile width
@@ -40,7 +43,7 @@ struct BlockTile {
 };
 
 template <bool STATS, bool CHECKED, bool SMEM, int TW, bool OCC>
-__global__ void __launch_bounds__(kBlock, OCC ? 5 : 1) k_render(WorldView w, FrameParams f, uint4* __restrict__ out,
+__global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldView w, FrameParams f, uint4* __restrict__ out,
                                                                unsigned* status, unsigned long long* counters) {
     // shared copy of the coarse bits for the model traversal (STATS or
     // CHECKED); the production walk reads the chunk distances through L1,
