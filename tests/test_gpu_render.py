@@ -283,3 +283,41 @@ def test_world_edits_match_oracle(vt, oracle, ctx):
     gpu = vt.render_host(ctx, w, cam, p)
     assert not (gpu["flags"] & vt.HIT_PRIMARY).any()
     w.close()
+
+
+def test_deferred_bounce_pass_equals_inline(vt, ctx):
+    """Bounce rays of vt_render / vt_render_host go through the deferred pass
+    (queue, persistent refill kernel, shading kernel); a batch job traces them
+    inline.  Records must be identical, also for two deferred frames queued
+    back to back on different streams (they share the context's queue)."""
+    d = vt.gen_desc((256, 160, 256), seed=12, trees=80, caves=True)
+    w = make_world(vt, ctx, vt.gen_world(d))
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW | vt.RAYS_BOUNCE, seed=5, sun_dir=vt.gen_sun(12))
+    cams = [vt.gen_camera(d, cs, 640, 400) for cs in range(2)]
+    inline = []
+    for cam in cams:
+        buf = ctx.alloc(cam.width * cam.height * 16)
+        b = vt.Batch(ctx, [(w, cam, buf)], p)
+        b.launch()
+        ctx.sync()
+        inline.append(buf.download(np.zeros(cam.width * cam.height, vt.HIT_DTYPE)))
+        b.close()
+        buf.free()
+    s1, s2 = ctx.stream(), ctx.stream()
+    bufs = [ctx.alloc(c.width * c.height * 16) for c in cams]
+    try:
+        vt.render(ctx, w, cams[0], p, bufs[0], s1)
+        vt.render(ctx, w, cams[1], p, bufs[1], s2)
+        ctx.sync(s1)
+        ctx.sync(s2)
+        for c, buf, want in zip(cams, bufs, inline):
+            got = buf.download(np.zeros(c.width * c.height, vt.HIT_DTYPE))
+            assert np.array_equal(got, want)
+            assert ((got["flags"] & vt.HIT_BOUNCE) != 0).sum() > 1000
+            assert np.array_equal(vt.render_host(ctx, w, c, p), want)
+    finally:
+        for b in bufs:
+            b.free()
+        for s in (s1, s2):
+            ctx.lib.vt_stream_destroy(ctx.handle, s)
+        w.close()

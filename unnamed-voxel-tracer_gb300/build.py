@@ -23,7 +23,7 @@ OUT_DIR = HERE / "lib"
 OBJ_DIR = HERE / "_build"
 LIB = OUT_DIR / "libvt.so"
 
-CUDA_SOURCES = ["api.cu", "world.cu", "render.cu", "tune.cu", "render_static.cu", "adjoint.cu", "batch.cu", "refmode.cu", "world_gen.cu", "edit.cu"]
+CUDA_SOURCES = ["api.cu", "world.cu", "render.cu", "tune.cu", "render_static.cu", "adjoint.cu", "batch.cu", "refmode.cu", "world_gen.cu", "edit.cu", "bounce.cu"]
 CXX_SOURCES = ["gen.cpp", "vox.cpp", "procgen_ref.cpp"]
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"

@@ -118,6 +118,10 @@ vt_status vt_ctx_destroy(vt_ctx* ctx) {
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    if (ctx->d_bounce_jobs) cudaFree(ctx->d_bounce_jobs);
+    if (ctx->d_bounce_open) cudaFree(ctx->d_bounce_open);
+    if (ctx->d_bounce_ctr) cudaFree(ctx->d_bounce_ctr);
+    if (ctx->ev_bounce) cudaEventDestroy(ctx->ev_bounce);
     for (int i = 0; i < kMaxBands; ++i)
         if (ctx->ev_band[i]) cudaEventDestroy(ctx->ev_band[i]);
     if (ctx->d_scratch) cudaFree(ctx->d_scratch);

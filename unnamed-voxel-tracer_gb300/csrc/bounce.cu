@@ -1,0 +1,120 @@
+// bounce.cu -- the deferred bounce pass (see bounce.cuh): a persistent
+// kernel that traces the queued bounce rays with per-lane refill, and a kernel
+// that shades the pixels whose bounce ray was deferred.
+#include "bounce.cuh"
+#include "trace_p.cuh"
+
+namespace vt {
+
+namespace {
+
+constexpr int kBounceBlock = 256;
+// a warp takes new rays from the queue once this many of its lanes are idle
+// (1, 4, 8, 16, 24 measured on a 4K cave-world frame: 8 is fastest)
+constexpr int kRefill = 8;
+
+// Persistent: every warp loops until the queue is drained.  A lane walks one
+// ray at a time, an iteration of the walk per loop turn; open[j] receives 1
+// when ray j leaves without a hit (the sky lights its pixel), 0 otherwise.
+__global__ void __launch_bounds__(kBounceBlock) k_bounce_trace(WorldView w, const BounceJob* __restrict__ jobs,
+                                                               const unsigned* __restrict__ counters,
+                                                               unsigned* __restrict__ next, unsigned char* open,
+                                                               int max_steps) {
+    const unsigned total = counters[0];
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned below = (1u << lane) - 1u;
+    Walker wk;
+    bool busy = false;
+    unsigned job = 0;
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xFFFFFFFFu, !busy);
+        if (idle == 0xFFFFFFFFu || __popc(idle) >= kRefill) {
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(next, (unsigned)__popc(idle));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base >= total && idle == 0xFFFFFFFFu) break;  // drained, and nothing in flight
+            if (!busy) {
+                job = base + (unsigned)__popc(idle & below);
+                if (job < total) {
+                    const BounceJob J = jobs[job];
+                    busy = wk.start(w, J.o, J.d, max_steps);
+                    if (!busy) open[job] = 1;  // misses the grid or may take no step
+                }
+            }
+        }
+        if (busy) {
+            TraceHit h;
+            const int s = wk.step<false, true, true>(w, w.cdist, h);
+            if (s != Walker::kMore) {
+                open[job] = s == Walker::kHit ? 0 : 1;
+                busy = false;
+            }
+        }
+    }
+}
+
+// One thread per deferred pixel: the shading render_pixel would have done with
+// this bounce result, and the record's rgba and VT_HIT_BOUNCE flag.
+__global__ void __launch_bounds__(kBounceBlock) k_bounce_finish(WorldView w, FrameParams f,
+                                                                const BounceJob* __restrict__ jobs,
+                                                                const unsigned* __restrict__ counters,
+                                                                const unsigned char* __restrict__ open,
+                                                                uint4* __restrict__ out) {
+    const unsigned total = counters[0];
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x) {
+        const BounceJob J = jobs[j];
+        const unsigned p = J.pixel;
+        const int px = (int)(p % (unsigned)f.width), py = (int)(p / (unsigned)f.width);
+        uint4 r = out[p];
+        const unsigned face = r.w & 0xFFu, mat = (r.w >> 8) & 0xFFu;
+        unsigned flags = (r.w >> 16) & 0xFFu;
+        const bool shadowed = (flags & (VT_HIT_SHADOWED | VT_HIT_ENTITY)) != 0u;
+        const bool bounce_open = open[j] != 0;
+        if (!bounce_open) flags |= VT_HIT_BOUNCE;
+        const unsigned alb = __ldg(w.palette + mat);
+        float col[4];
+        shade_hit(f, alb, (int)(face >> 1), (face & 1u) == 0u, shadowed, bounce_open, J.d, col);
+        r.z = f.shade == VT_SHADE_NONE ? alb : composite(f, px, py, col);
+        r.w = face | (mat << 8) | (flags << 16);
+        out[p] = r;
+    }
+}
+
+}  // namespace
+
+vt_status bounce_buffers(vt_ctx* ctx, size_t pixels) {
+    if (pixels <= ctx->bounce_capacity) return VT_OK;
+    VT_CUDA(ctx, cudaDeviceSynchronize());
+    if (ctx->d_bounce_jobs) cudaFree(ctx->d_bounce_jobs);
+    if (ctx->d_bounce_open) cudaFree(ctx->d_bounce_open);
+    ctx->d_bounce_jobs = nullptr;
+    ctx->d_bounce_open = nullptr;
+    ctx->bounce_capacity = 0;
+    VT_CUDA(ctx, cudaMalloc(&ctx->d_bounce_jobs, pixels * sizeof(BounceJob)));
+    VT_CUDA(ctx, cudaMalloc(&ctx->d_bounce_open, pixels));
+    if (!ctx->d_bounce_ctr) VT_CUDA(ctx, cudaMalloc(&ctx->d_bounce_ctr, 2 * sizeof(unsigned)));
+    if (!ctx->ev_bounce) VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_bounce, cudaEventDisableTiming));
+    ctx->bounce_capacity = pixels;
+    return VT_OK;
+}
+
+vt_status launch_bounce(vt_ctx* ctx, const vt_world* world, const FrameParams& f, uint4* d_out, cudaStream_t st) {
+    const WorldView w = world->view();
+    if (ctx->bounce_blocks == 0) {
+        int nb = 0;
+        VT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bounce_trace, kBounceBlock, 0));
+        ctx->bounce_blocks = ctx->sm_count * (nb > 0 ? nb : 1);
+    }
+    const BounceJob* jobs = reinterpret_cast<const BounceJob*>(ctx->d_bounce_jobs);
+    k_bounce_trace<<<ctx->bounce_blocks, kBounceBlock, 0, st>>>(w, jobs, ctx->d_bounce_ctr, ctx->d_bounce_ctr + 1,
+                                                                ctx->d_bounce_open, f.bounce_max_steps);
+    VT_CUDA(ctx, cudaGetLastError());
+    k_bounce_finish<<<ctx->sm_count * 8, kBounceBlock, 0, st>>>(w, f, jobs, ctx->d_bounce_ctr, ctx->d_bounce_open,
+                                                                d_out);
+    VT_CUDA(ctx, cudaGetLastError());
+    // the next deferred frame of this context reuses the queue after this one
+    VT_CUDA(ctx, cudaEventRecord(ctx->ev_bounce, st));
+    return VT_OK;
+}
+
+}  // namespace vt

@@ -270,6 +270,8 @@ FrameParams make_frame(const vt_camera* cam, const vt_params* p) {
     f.height = cam->height;
     f.row0 = 0;
     f.row_end = cam->height;
+    f.bounce_jobs = nullptr;
+    f.bounce_count = nullptr;
     f.max_steps = p->max_steps;
     f.shadow_max_steps = p->shadow_max_steps;
     f.bounce_max_steps = p->bounce_max_steps;
@@ -314,7 +316,7 @@ vt_status band_streams(vt_ctx* ctx) {
 }
 
 vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p,
-                               uint4* d_out, cudaStream_t stream, bool stats, int row0, int row1) {
+                               uint4* d_out, cudaStream_t stream, bool stats, int row0, int row1, bool allow_defer) {
     FrameParams f = make_frame(cam, p);
     if (row1 < 0) row1 = cam->height;
     f.row0 = row0;
@@ -351,6 +353,15 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         VT_CUDA(ctx, cudaGetLastError());
         return VT_OK;
     }
+    const bool defer = allow_defer && (p->rays & VT_RAYS_BOUNCE) && !stats && !checked;
+    if (defer) {
+        vt_status s = bounce_buffers(ctx, (size_t)cam->width * (size_t)cam->height);
+        if (s) return s;
+        VT_CUDA(ctx, cudaStreamWaitEvent(stream, ctx->ev_bounce, 0));
+        VT_CUDA(ctx, cudaMemsetAsync(ctx->d_bounce_ctr, 0, 2 * sizeof(unsigned), stream));
+        f.bounce_jobs = ctx->d_bounce_jobs;
+        f.bounce_count = ctx->d_bounce_ctr;
+    }
 #define VT_LAUNCH(S, C, M, TW, O)                                                                               \
     k_render<S, C, M, TW, O><<<dim3((cam->width + BlockTile<TW>::kW - 1) / BlockTile<TW>::kW,                   \
                                     (rows + BlockTile<TW>::kH - 1) / BlockTile<TW>::kH),                        \
@@ -375,6 +386,7 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
 #undef VT_LAUNCH_M
 #undef VT_LAUNCH
     VT_CUDA(ctx, cudaGetLastError());
+    if (defer) return launch_bounce(ctx, world, f, d_out, stream);
     return VT_OK;
 }
 
@@ -408,7 +420,8 @@ vt_status vt_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, co
     vt_status s = check_frame_args(ctx, world, cam, params);
     if (s) return s;
     if (!d_out) return fail(ctx, VT_ERR_ARG, "null output buffer");
-    return launch_render(ctx, world, cam, params, reinterpret_cast<uint4*>(d_out), (cudaStream_t)stream, false);
+    return launch_render(ctx, world, cam, params, reinterpret_cast<uint4*>(d_out), (cudaStream_t)stream, false, 0, -1,
+                         true);
 }
 
 vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* params,
@@ -425,7 +438,8 @@ vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* ca
     {
         cudaPointerAttributes pa;
         if (cudaPointerGetAttributes(&pa, h_out) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {
-            s = launch_render(ctx, world, cam, params, reinterpret_cast<uint4*>(pa.devicePointer), ctx->stream, false);
+            s = launch_render(ctx, world, cam, params, reinterpret_cast<uint4*>(pa.devicePointer), ctx->stream, false,
+                              0, -1, true);
             if (s) return s;
             return vt_sync(ctx, ctx->stream);
         }
@@ -436,10 +450,12 @@ vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* ca
     if (s) return s;
     uint4* d_out = reinterpret_cast<uint4*>(d_scratch);
     const int rows_tile = band_rows_unit(ctx->tuning);
+    // (bounce rays go through the deferred pass, one launch for the frame)
     const bool pipelined = ctx->tuning.kernel == VT_KERNEL_TILE && W * H >= kPipelinePixels &&
-                           (params->flags & VT_FLAG_CHECKED) == 0 && rows_tile > 0;
+                           (params->flags & VT_FLAG_CHECKED) == 0 && (params->rays & VT_RAYS_BOUNCE) == 0 &&
+                           rows_tile > 0;
     if (!pipelined) {
-        s = launch_render(ctx, world, cam, params, d_out, ctx->stream, false);
+        s = launch_render(ctx, world, cam, params, d_out, ctx->stream, false, 0, -1, true);
         if (s) return s;
         VT_CUDA(ctx, cudaMemcpyAsync(h_out, d_out, bytes, cudaMemcpyDeviceToHost, ctx->stream));
         return vt_sync(ctx, ctx->stream);

@@ -3,6 +3,7 @@
 // the batched kernels.
 #pragma once
 
+#include "bounce.cuh"
 #include "shade.cuh"
 #include "trace_p.cuh"
 
@@ -81,10 +82,17 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
             }
         }
         bool bounce_open = false;
+        bool deferred = false;
         float bdir[3] = {0.0f, 0.0f, 0.0f};
         if (f.rays & VT_RAYS_BOUNCE) {
             unsigned seed = ((unsigned)px * 1973u + (unsigned)py * 9277u) ^ f.seed;
             cosine_hemisphere(nrm, seed, bdir);
+            deferred = !STATS && !CHECKED && f.bounce_jobs != nullptr;
+        }
+        if (deferred) {
+            // traced and shaded by the bounce kernels (bounce.cu)
+            append_bounce(f, so, bdir, (unsigned)py * (unsigned)f.width + (unsigned)px);
+        } else if (f.rays & VT_RAYS_BOUNCE) {
             PRay rb;
             pray_init(rb, so, bdir);
             TraceHit hb;
@@ -96,8 +104,12 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
                 pc.v[5] += bh ? 1u : 0u;
             }
         }
-        shade_hit(f, alb, e, pe, shadowed, bounce_open, bdir, col);
-        rgba = f.shade == VT_SHADE_NONE ? alb : composite(f, px, py, col);
+        if (deferred) {
+            rgba = 0u;
+        } else {
+            shade_hit(f, alb, e, pe, shadowed, bounce_open, bdir, col);
+            rgba = f.shade == VT_SHADE_NONE ? alb : composite(f, px, py, col);
+        }
     } else {
         shade_miss(f, d, col);
         rgba = f.shade == VT_SHADE_NONE ? 0u : composite(f, px, py, col);

@@ -31,6 +31,8 @@ struct FrameParams {
     float lit_sky[3];   // SkyDome2 of the RGBA8-stored sun direction (blit.fragment.glsl:31)
     float lit_a;        // illumination alpha 0.3 stored in RGBA8
     int row0, row_end;  // rows [row0, row_end) of the image this launch renders
+    void* bounce_jobs;       // non-null: bounce rays are queued here (BounceJob), not traced inline
+    unsigned* bounce_count;  // the queue's length
 };
 
 __device__ __forceinline__ void primary_ray(const FrameParams& f, int px, int py, float o[3], float d[3]) {

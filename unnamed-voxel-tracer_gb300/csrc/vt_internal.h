@@ -87,6 +87,13 @@ struct vt_ctx {
     cudaEvent_t ev_start = nullptr;
     cudaEvent_t ev_band[16] = {};
     unsigned* h_status = nullptr;  // pinned copy of d_status
+    // the deferred bounce pass (bounce.cu): ray queue, results, counters
+    void* d_bounce_jobs = nullptr;
+    unsigned char* d_bounce_open = nullptr;
+    unsigned* d_bounce_ctr = nullptr;  // {queued, taken}
+    size_t bounce_capacity = 0;
+    cudaEvent_t ev_bounce = nullptr;   // the last deferred frame is done with the queue
+    int bounce_blocks = 0;
 };
 
 namespace vt {
@@ -166,8 +173,16 @@ vt_status world_stage(vt_world* w, size_t bytes, unsigned char** out);
 vt_status check_frame_args(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p);
 // Queues one frame (render kernel, distances rebuilt first if stale) writing
 // width*height records to d_out on `stream`.
+// allow_defer: bounce rays may go through the context's deferred bounce pass
+// (single-frame entry points; not inside graph capture or allocation-free
+// calls).
 vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p, uint4* d_out,
-                        cudaStream_t stream, bool stats, int row0 = 0, int row1 = -1);
+                        cudaStream_t stream, bool stats, int row0 = 0, int row1 = -1, bool allow_defer = false);
+struct FrameParams;
+// The deferred bounce pass: queue buffers for `pixels` rays, and the trace +
+// shade kernels for a frame whose render kernel queued them.
+vt_status bounce_buffers(vt_ctx* ctx, size_t pixels);
+vt_status launch_bounce(vt_ctx* ctx, const vt_world* world, const FrameParams& f, uint4* d_out, cudaStream_t st);
 }  // namespace vt
 
 #define VT_CUDA(ctx, call)                                                      \
