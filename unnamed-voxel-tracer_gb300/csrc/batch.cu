@@ -40,7 +40,7 @@ constexpr int kUnit = 16;  // pixels per unit side
 #endif
 constexpr int kBatchChains = VT_BATCH_CHAINS;
 
-__global__ void __launch_bounds__(kBatchBlock, 4) k_render_batch(const JobDesc* __restrict__ jobs, int njobs,
+__global__ void __launch_bounds__(kBatchBlock, 3) k_render_batch(const JobDesc* __restrict__ jobs, int njobs,
                                                                  unsigned total_units, unsigned* __restrict__ counter) {
     const unsigned lane = threadIdx.x & 31u;
     for (;;) {
@@ -57,8 +57,10 @@ __global__ void __launch_bounds__(kBatchBlock, 4) k_render_batch(const JobDesc* 
         const JobDesc& J = jobs[lo];
         const unsigned local = unit - J.first_unit;
         const int ux = (int)(local % J.units_x) * kUnit, uy = (int)(local / J.units_x) * kUnit;
-        const WorldView w = J.w;
-        const FrameParams f = J.f;
+        // world and frame are read from the job table in place (L1-cached):
+        // copying the two structs into registers spills
+        const WorldView& w = J.w;
+        const FrameParams& f = J.f;
         for (int sub = 0; sub < 8; ++sub) {
             const int px = ux + (sub & 1) * 8 + (int)(lane & 7u);
             const int py = uy + (sub >> 1) * 4 + (int)(lane >> 3);
