@@ -323,7 +323,8 @@ def measure_mode_r(vt, ctx, torch, mats, cams, flush) -> dict:
 
 def measure_config4(vt, scenes, ctx, torch) -> dict:
     """256^3 world, 16 views at 512x512: one optimisation step = fused
-    forward + backward of the shading (shadow rays recomputed) over all views."""
+    forward + backward of the shading (shadow rays recomputed) over all views,
+    one vt_shade_backward_views call."""
     desc, cams, (pal, alb, sun), (hpal, hsun) = scenes.config4()
     w = vt.World(ctx, tuple(desc.dims))
     w.upload_dense(vt.gen_world(desc))
@@ -342,8 +343,7 @@ def measure_config4(vt, scenes, ctx, torch) -> dict:
 
     def step():
         sh_.zero_grad_async()
-        for c, hb, tb in zip(cams, hits, targets):
-            sh_.backward(c, hb, tb)
+        sh_.backward_views(cams, hits, targets)
 
     def forward():
         for c, hb in zip(cams, hits):

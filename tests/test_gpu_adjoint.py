@@ -130,3 +130,29 @@ def test_backward_matches_finite_differences(vt, ctx, scene):
     sh.set_params(s["pal"], s["alb"], s["sun"])
     for b in (rgb, vis, dt):
         b.free()
+
+
+def test_backward_views_equals_per_view_calls(vt, ctx, scene):
+    """The multi-view call (views on concurrent streams) accumulates the same
+    loss and gradients as one call per view, up to the order of the float
+    atomics."""
+    s = scene
+    sh = s["sh"]
+    tgts = []
+    for tgt in s["targets"]:
+        dt = ctx.alloc(tgt.nbytes)
+        dt.upload(tgt)
+        tgts.append(dt)
+    sh.zero_grad()
+    for cam, hb, dt in zip(s["cams"], s["hits"], tgts):
+        sh.backward(cam, hb, dt)
+    one = sh.grads()
+    sh.zero_grad()
+    sh.backward_views(s["cams"], s["hits"], tgts)
+    many = sh.grads()
+    for k in ("palette", "sun"):
+        scale = np.abs(one[k]).max()
+        assert np.abs(many[k] - one[k]).max() <= 1e-5 * scale, k
+    assert abs(many["loss"] - one["loss"]) <= 1e-5 * abs(one["loss"])
+    for dt in tgts:
+        dt.free()

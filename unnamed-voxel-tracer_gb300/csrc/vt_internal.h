@@ -182,6 +182,8 @@ struct FrameParams;
 // The deferred bounce pass: queue buffers for `pixels` rays, and the trace +
 // shade kernels for a frame whose render kernel queued them.
 vt_status bounce_buffers(vt_ctx* ctx, size_t pixels);
+// The context's band streams and events (created on first use).
+vt_status band_streams(vt_ctx* ctx);
 vt_status launch_bounce(vt_ctx* ctx, const vt_world* world, const FrameParams& f, uint4* d_out, cudaStream_t st);
 }  // namespace vt
 

@@ -137,6 +137,8 @@ _SIGNATURES = {
     "vt_trace_rays": (_S, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, _P]),
     "vt_shade_forward": (_S, [_P, _P, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P, _P, _P]),
     "vt_shade_backward": (_S, [_P, _P, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P, _P, _P, _P, _P]),
+    "vt_shade_backward_views": (_S, [_P, _P, C.c_int32, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P,
+                                     _P, _P, _P, _P]),
     "vt_brickmap_create": (_S, [_P, C.POINTER(_P)]),
     "vt_brickmap_destroy": (_S, [_P]),
     "vt_brickmap_upload": (_S, [_P, _P, _P, C.c_size_t]),
@@ -639,6 +641,16 @@ class Shading:
             self.ctx.handle, self.world.handle, C.byref(cam), d_hits.ptr, C.byref(self.inputs), d_target.ptr,
             self.d_loss.ptr, self.d_gpal.ptr, self.d_galb.ptr if self.d_galb is not None else None,
             self.d_gsun.ptr, stream))
+
+    def backward_views(self, cams, d_hits, d_targets, stream=None) -> None:
+        """backward over many views in one call (concurrent internally)."""
+        n = len(cams)
+        cam_arr = (Camera_t * n)(*cams)
+        hits = (C.c_void_p * n)(*[h.ptr for h in d_hits])
+        tgts = (C.c_void_p * n)(*[t.ptr for t in d_targets])
+        self.ctx.check(self.ctx.lib.vt_shade_backward_views(
+            self.ctx.handle, self.world.handle, n, cam_arr, hits, C.byref(self.inputs), tgts, self.d_loss.ptr,
+            self.d_gpal.ptr, self.d_galb.ptr if self.d_galb is not None else None, self.d_gsun.ptr, stream))
 
     def grads(self) -> dict:
         self.ctx.sync()
