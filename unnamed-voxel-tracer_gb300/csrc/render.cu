@@ -16,7 +16,7 @@ namespace vt {
 
 // 256-thread blocks; each warp traces a compact pixel tile so that its rays
 // start close together and share brick words in L1.
-constexpr int kBlock = 256;
+constexpr int kBlock = 256;  // 128 measured the same with the register cap
 constexpr size_t kMaxSharedCoarse = 48 * 1024;
 
 template <bool STATS>
@@ -34,12 +34,12 @@ __device__ __forceinline__ void flush_counters(PixelCounters& pc, unsigned long 
 // budget so that kOccBlocks blocks fit on an SM: 4 blocks (64 registers, 32
 // warps, no spills) measured 4% faster on a 1080p frame than 5 (48 registers
 // with spills) and 3 (uncapped, 67 registers).
-constexpr int kOccBlocks = 4;
+constexpr int kOccBlocks = 4 * 256 / kBlock;
 template <int TW>
 struct BlockTile {
     static constexpr int kW = TW < 16 ? 16 : TW;     // block tile width
     static constexpr int kWarpsX = kW / TW;
-    static constexpr int kH = (8 / kWarpsX) * (32 / TW);
+    static constexpr int kH = (kBlock / 32 / kWarpsX) * (32 / TW);
 };
 
 template <bool STATS, bool CHECKED, bool SMEM, int TW, bool OCC>
