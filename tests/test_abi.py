@@ -139,3 +139,16 @@ def test_no_device_here_is_an_error_not_a_crash(vtlib):
         lib.vt_ctx_destroy(h)
         pytest.skip("a GPU is present")
     assert st == 6
+
+
+def test_unorm8_table():
+    """The device table of float(i) / 255.0f (unorm8.cuh) against the IEEE
+    division, entry by entry."""
+    import re
+    from pathlib import Path
+    src = (Path(__file__).resolve().parent.parent / "unnamed-voxel-tracer_gb300" / "csrc" / "unorm8.cuh").read_text()
+    body = src[src.index("kUnorm8[256] = {"):src.index("};")]
+    vals = [float.fromhex(m) for m in re.findall(r"(0x[0-9a-fp.+-]+)f", body)]
+    assert len(vals) == 256
+    want = np.arange(256, dtype=np.float32) / np.float32(255)
+    assert np.array_equal(np.array(vals, np.float32).view(np.uint32), want.view(np.uint32))

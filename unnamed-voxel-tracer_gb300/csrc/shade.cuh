@@ -12,6 +12,7 @@
 // Compiled with --fmad=false: every expression rounds as written.
 #pragma once
 
+#include "unorm8.cuh"
 #include "vt_internal.h"
 
 namespace vt {
@@ -106,6 +107,20 @@ __host__ __device__ __forceinline__ void sky(const float sun[3], const float rd[
     col[2] = ((0.75f - dy * 1.0f) + (0.15f * 0.5f)) + (0.4f * 0.1f) * s8 + 0.04f * s3;
 }
 
+// sky() with the sun direction already normalised (FrameParams::sun_n, made
+// on the host by the same normalize3): the same value without the per-call
+// normalisation of the sun.
+__device__ __forceinline__ void sky_n(const float sn[3], const float rd[3], float col[3]) {
+    float rn[3];
+    normalize3(rd, rn);
+    const float s = clampf(dot3(sn, rn), 0.0f, 1.2f);
+    const float s2 = s * s, s3 = s2 * s, s4 = s2 * s2, s8 = s4 * s4;
+    const float dy = rd[1] * 0.2f;
+    col[0] = ((0.6f - dy * 1.0f) + (0.15f * 0.5f)) + (0.4f * 1.0f) * s8 + 0.2f * s3;
+    col[1] = ((0.71f - dy * 0.5f) + (0.15f * 0.5f)) + (0.4f * 0.6f) * s8 + 0.08f * s3;
+    col[2] = ((0.75f - dy * 1.0f) + (0.15f * 0.5f)) + (0.4f * 0.1f) * s8 + 0.04f * s3;
+}
+
 __device__ __forceinline__ float vignette(int px, int py, int W, int H) {
     const float u = ((float)px + 0.5f) / (float)W;
     const float v = ((float)py + 0.5f) / (float)H;
@@ -186,7 +201,7 @@ __device__ __forceinline__ void shade_hit(const FrameParams& f, unsigned alb, in
                                           bool bounce_open, const float bdir[3], float col[4]) {
     float albf[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) albf[j] = (float)((alb >> (8 * j)) & 255u) / 255.0f;
+    for (int j = 0; j < 4; ++j) albf[j] = unorm8_to_float((alb >> (8 * j)) & 255u);
     if (f.shade == VT_SHADE_REFERENCE) {
         const float a = shadowed ? 0.0f : f.lit_a;
 #pragma unroll
@@ -194,7 +209,7 @@ __device__ __forceinline__ void shade_hit(const FrameParams& f, unsigned alb, in
         col[3] = albf[3] + a * 1.0f;
         if (bounce_open) {
             float bc[3];
-            sky(f.sun, bdir, bc);
+            sky_n(f.sun_n, bdir, bc);
 #pragma unroll
             for (int j = 0; j < 3; ++j) col[j] = col[j] + f.bounce_weight * (albf[j] * bc[j]);
         }
@@ -220,9 +235,9 @@ __device__ __forceinline__ void shade_miss(const FrameParams& f, const float d[3
     col[0] = col[1] = col[2] = col[3] = 0.0f;
     if (f.shade == VT_SHADE_REFERENCE) {
         float sc[3];
-        sky(f.sun, d, sc);
+        sky_n(f.sun_n, d, sc);
 #pragma unroll
-        for (int j = 0; j < 3; ++j) col[j] = (float)unorm8(sc[j]) / 255.0f;
+        for (int j = 0; j < 3; ++j) col[j] = unorm8_to_float(unorm8(sc[j]));
         col[3] = 1.0f;
     }
 }
