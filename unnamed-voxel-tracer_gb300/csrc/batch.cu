@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(kBatchBlock, 3) k_render_batch(const JobDesc* 
             if (px < f.width && py < f.height) {
                 PixelCounters pc;
                 J.out[(size_t)py * f.width + px] =
-                    render_pixel<false, false>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, nullptr, pc);
+                    render_pixel<false, false>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, pixel_uv(f, px, py),
+                                               nullptr, pc);
             }
         }
     }

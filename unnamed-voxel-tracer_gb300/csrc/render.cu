@@ -40,6 +40,7 @@ struct BlockTile {
     static constexpr int kW = TW < 16 ? 16 : TW;     // block tile width
     static constexpr int kWarpsX = kW / TW;
     static constexpr int kH = (kBlock / 32 / kWarpsX) * (32 / TW);
+    static_assert(kW <= 64 && kH <= kBlock - 64, "the column and row tables are filled by distinct threads");
 };
 
 template <bool STATS, bool CHECKED, bool SMEM, int TW, bool OCC>
@@ -50,21 +51,36 @@ __global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldVi
     // which measured faster than staging all 8 octant fields per block
     extern __shared__ uint4 s_dyn[];
     unsigned long long* s_coarse = reinterpret_cast<unsigned long long*>(s_dyn);
-    if (SMEM) {
-        for (unsigned i = threadIdx.x; i < w.ncoarse; i += blockDim.x) s_coarse[i] = __ldg(w.coarse + i);
-        __syncthreads();
-    }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     using BT = BlockTile<TW>;
-    const int px = blockIdx.x * BT::kW + (warp % BT::kWarpsX) * TW + (lane % TW);
-    const int py = f.row0 + blockIdx.y * BT::kH + (warp / BT::kWarpsX) * (32 / TW) + (lane / TW);
+    // screen coordinates of the block's columns and rows, once per block
+    // instead of four divisions per pixel
+    __shared__ float s_col[2][BT::kW], s_row[2][BT::kH];
+    const int x0 = blockIdx.x * BT::kW, y0 = f.row0 + blockIdx.y * BT::kH;
+    if (threadIdx.x < BT::kW) {
+        s_col[0][threadIdx.x] = ray_u(f, x0 + (int)threadIdx.x);
+        s_col[1][threadIdx.x] = centre_u(f, x0 + (int)threadIdx.x);
+    } else if (threadIdx.x >= 64 && threadIdx.x < 64 + BT::kH) {
+        s_row[0][threadIdx.x - 64] = ray_v(f, y0 + (int)threadIdx.x - 64);
+        s_row[1][threadIdx.x - 64] = centre_v(f, y0 + (int)threadIdx.x - 64);
+    }
+    if (SMEM)
+        for (unsigned i = threadIdx.x; i < w.ncoarse; i += blockDim.x) s_coarse[i] = __ldg(w.coarse + i);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int lx = (warp % BT::kWarpsX) * TW + (lane % TW), ly = (warp / BT::kWarpsX) * (32 / TW) + (lane / TW);
+    const int px = x0 + lx, py = y0 + ly;
     PixelCounters pc;
 #pragma unroll
     for (int k = 0; k < kNumCounters; ++k) pc.v[k] = 0;
     if (px < f.width && py < f.row_end) {
+        PixelUV uv;
+        uv.ru = s_col[0][lx];
+        uv.cu = s_col[1][lx];
+        uv.rv = s_row[0][ly];
+        uv.cv = s_row[1][ly];
         uint4 rec;
-        if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, w.cdist, f, px, py, status, pc);
-        else rec = render_pixel<STATS, CHECKED>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, status, pc);
+        if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, w.cdist, f, px, py, uv, status, pc);
+        else rec = render_pixel<STATS, CHECKED>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, uv, status, pc);
         out[(size_t)py * f.width + px] = rec;
     }
     flush_counters<STATS>(pc, counters);

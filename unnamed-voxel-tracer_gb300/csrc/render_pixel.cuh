@@ -27,12 +27,14 @@ __device__ __forceinline__ bool trace_any(const WorldView& w, const Coarse& coar
     return trace_fast<MAT, true, false>(w, cd, r, max_steps, h);
 }
 
+// uv: the pixel's screen coordinates (pixel_uv(f, px, py); the frame kernel
+// reads them from per-block tables).
 template <bool STATS, bool CHECKED, class Coarse>
 __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
-                                              const FrameParams& f, int px, int py, unsigned* status,
-                                              PixelCounters& pc) {
+                                              const FrameParams& f, int px, int py, const PixelUV& uv,
+                                              unsigned* status, PixelCounters& pc) {
     float o[3], d[3];
-    primary_ray(f, px, py, o, d);
+    primary_ray_uv(f, uv, o, d);
     PRay r;
     pray_init(r, o, d);
     TraceHit h;
@@ -108,11 +110,11 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
             rgba = 0u;
         } else {
             shade_hit(f, alb, e, pe, shadowed, bounce_open, bdir, col);
-            rgba = f.shade == VT_SHADE_NONE ? alb : composite(f, px, py, col);
+            rgba = f.shade == VT_SHADE_NONE ? alb : composite_uv(f, uv, col);
         }
     } else {
         shade_miss(f, d, col);
-        rgba = f.shade == VT_SHADE_NONE ? 0u : composite(f, px, py, col);
+        rgba = f.shade == VT_SHADE_NONE ? 0u : composite_uv(f, uv, col);
     }
     if (STATS) {
         pc.v[6] += cnt.mask;

@@ -36,13 +36,39 @@ struct FrameParams {
     unsigned* bounce_count;  // the queue's length
 };
 
-__device__ __forceinline__ void primary_ray(const FrameParams& f, int px, int py, float o[3], float d[3]) {
+// The per-pixel screen coordinates, each a function of the column or of the
+// row alone (so a block can compute them once per column and row).
+struct PixelUV {
+    float ru, rv;  // the primary ray's UV (primary.comp.glsl:31-36)
+    float cu, cv;  // the pixel centre in [0, 1] (vignette, crosshair)
+};
+
+__device__ __forceinline__ float ray_u(const FrameParams& f, int px) {
+    const float u = (((float)px / (float)f.width) * 2.0f) - 1.0f;
+    return u * f.tan_half_fov;
+}
+
+__device__ __forceinline__ float ray_v(const FrameParams& f, int py) {
     const float W = (float)f.width, H = (float)f.height;
-    float u = (((float)px / W) * 2.0f) - 1.0f;
     float v = (((float)py / H) * 2.0f) - 1.0f;
     v = v * (H / W);
-    u = u * f.tan_half_fov;
-    v = v * f.tan_half_fov;
+    return v * f.tan_half_fov;
+}
+
+__device__ __forceinline__ float centre_u(const FrameParams& f, int px) { return ((float)px + 0.5f) / (float)f.width; }
+__device__ __forceinline__ float centre_v(const FrameParams& f, int py) { return ((float)py + 0.5f) / (float)f.height; }
+
+__device__ __forceinline__ PixelUV pixel_uv(const FrameParams& f, int px, int py) {
+    PixelUV uv;
+    uv.ru = ray_u(f, px);
+    uv.rv = ray_v(f, py);
+    uv.cu = centre_u(f, px);
+    uv.cv = centre_v(f, py);
+    return uv;
+}
+
+__device__ __forceinline__ void primary_ray_uv(const FrameParams& f, const PixelUV& uv, float o[3], float d[3]) {
+    const float u = uv.ru, v = uv.rv;
     float q[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) q[j] = ((u * f.view[0 * 4 + j] + v * f.view[1 * 4 + j]) + f.view[2 * 4 + j]) + f.view[3 * 4 + j];
@@ -52,6 +78,10 @@ __device__ __forceinline__ void primary_ray(const FrameParams& f, int px, int py
         d[j] = __fdiv_rn(q[j], len);
         o[j] = f.pos[j];
     }
+}
+
+__device__ __forceinline__ void primary_ray(const FrameParams& f, int px, int py, float o[3], float d[3]) {
+    primary_ray_uv(f, pixel_uv(f, px, py), o, d);
 }
 
 // Entity occluders (the role of traceEntities, map.glsl:172-201, in the
@@ -121,16 +151,14 @@ __device__ __forceinline__ void sky_n(const float sn[3], const float rd[3], floa
     col[2] = ((0.75f - dy * 1.0f) + (0.15f * 0.5f)) + (0.4f * 0.1f) * s8 + 0.04f * s3;
 }
 
-__device__ __forceinline__ float vignette(int px, int py, int W, int H) {
-    const float u = ((float)px + 0.5f) / (float)W;
-    const float v = ((float)py + 0.5f) / (float)H;
+// u, v: the pixel centre in [0, 1] (PixelUV::cu, cv)
+__device__ __forceinline__ float vignette(float u, float v) {
     const float a = u * (1.0f - u), b = v * (1.0f - v);
     return powf(a * b * 15.0f, 0.18f);
 }
 
-__device__ __forceinline__ bool crosshair(int px, int py, int W, int H) {
-    const float u = ((float)px + 0.5f) / (float)W - 0.5f;
-    const float v = ((float)py + 0.5f) / (float)H - 0.5f;
+__device__ __forceinline__ bool crosshair(float cu, float cv) {
+    const float u = cu - 0.5f, v = cv - 0.5f;
     return __fsqrt_rn(u * u + v * v) <= 0.002f;
 }
 
@@ -242,21 +270,25 @@ __device__ __forceinline__ void shade_miss(const FrameParams& f, const float d[3
     }
 }
 
-__device__ __forceinline__ unsigned composite(const FrameParams& f, int px, int py, float col[4]) {
+__device__ __forceinline__ unsigned composite_uv(const FrameParams& f, const PixelUV& uv, float col[4]) {
     if (f.shade == VT_SHADE_REFERENCE) {
-        if ((f.flags & VT_FLAG_CROSSHAIR) && crosshair(px, py, f.width, f.height)) {
+        if ((f.flags & VT_FLAG_CROSSHAIR) && crosshair(uv.cu, uv.cv)) {
             col[0] = col[0] * 0.5f + 0.5f;
             col[1] = col[1] * 0.5f + 0.5f;
             col[2] = col[2] * 0.5f + 0.5f;
             col[3] = col[3] * 0.5f + 0.2f;
         }
         if (f.flags & VT_FLAG_VIGNETTE) {
-            const float g = vignette(px, py, f.width, f.height);
+            const float g = vignette(uv.cu, uv.cv);
 #pragma unroll
             for (int j = 0; j < 4; ++j) col[j] = g * col[j];
         }
     }
     return unorm8(col[0]) | (unorm8(col[1]) << 8) | (unorm8(col[2]) << 16) | (unorm8(col[3]) << 24);
+}
+
+__device__ __forceinline__ unsigned composite(const FrameParams& f, int px, int py, float col[4]) {
+    return composite_uv(f, pixel_uv(f, px, py), col);
 }
 
 // FrameParams of a camera and parameter set (render.cu).
