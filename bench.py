@@ -339,22 +339,21 @@ def measure_config4(vt, scenes, ctx, torch) -> dict:
         hidden.forward(c, hb, tb)
     hidden.close()
     sh_ = vt.Shading(ctx, w, pal, alb, sun)
-    rgb = ctx.alloc(n * 12)
+    rgbs = [ctx.alloc(n * 12) for _ in cams]
 
     def step():
         sh_.zero_grad_async()
         sh_.backward_views(cams, hits, targets)
 
     def forward():
-        for c, hb in zip(cams, hits):
-            sh_.forward(c, hb, rgb)
+        sh_.forward_views(cams, hits, rgbs)
 
     step()
     t_step = _timed(torch, step, 5)
     t_fwd = _timed(torch, forward, 5)
     loss = sh_.grads()["loss"]
     sh_.close()
-    for b in hits + targets + [rgb]:
+    for b in hits + targets + rgbs:
         b.free()
     w.close()
     return {"workload": "256^3 world, 16 views at 512x512, Lambert + shadowed sun, L2 image loss",

@@ -156,3 +156,18 @@ def test_backward_views_equals_per_view_calls(vt, ctx, scene):
     assert abs(many["loss"] - one["loss"]) <= 1e-5 * abs(one["loss"])
     for dt in tgts:
         dt.free()
+
+
+def test_forward_views_equals_per_view_calls(vt, ctx, scene):
+    s = scene
+    n = s["cams"][0].width * s["cams"][0].height
+    one = [ctx.alloc(n * 12) for _ in s["cams"]]
+    many = [ctx.alloc(n * 12) for _ in s["cams"]]
+    for cam, hb, rb in zip(s["cams"], s["hits"], one):
+        s["sh"].forward(cam, hb, rb)
+    s["sh"].forward_views(s["cams"], s["hits"], many)
+    ctx.sync()
+    for a, b in zip(one, many):
+        assert np.array_equal(a.download(np.zeros(n * 3, np.float32)), b.download(np.zeros(n * 3, np.float32)))
+    for b in one + many:
+        b.free()

@@ -269,6 +269,30 @@ vt_status vt_shade_backward(vt_ctx* ctx, const vt_world* world, const vt_camera*
     return launch_shade(ctx, world, cam, d_hits, in, a, true, (cudaStream_t)stream);
 }
 
+vt_status vt_shade_forward_views(vt_ctx* ctx, const vt_world* world, int32_t n, const vt_camera* cams,
+                                 const vt_hit* const* d_hits, const vt_shade_inputs* in, float* const* d_rgb,
+                                 vt_stream stream) {
+    if (!ctx) return VT_ERR_ARG;
+    if (n < 0 || (n > 0 && (!cams || !d_hits || !d_rgb))) return fail(ctx, VT_ERR_ARG, "bad view lists");
+    if (n == 0) return VT_OK;
+    vt_status s = band_streams(ctx);
+    if (s) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    s = update_distances(const_cast<vt_world*>(world), st);
+    if (s) return s;
+    VT_CUDA(ctx, cudaEventRecord(ctx->ev_start, st));
+    const int k = n < kBandStreams ? n : kBandStreams;
+    for (int i = 0; i < k; ++i) VT_CUDA(ctx, cudaStreamWaitEvent(ctx->band_stream[i], ctx->ev_start, 0));
+    for (int v = 0; v < n && !s; ++v)
+        s = vt_shade_forward(ctx, world, &cams[v], d_hits[v], in, nullptr, nullptr, d_rgb[v],
+                             ctx->band_stream[v % kBandStreams]);
+    for (int i = 0; i < k; ++i) {
+        VT_CUDA(ctx, cudaEventRecord(ctx->ev_band[i], ctx->band_stream[i]));
+        VT_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_band[i], 0));
+    }
+    return s;
+}
+
 vt_status vt_shade_backward_views(vt_ctx* ctx, const vt_world* world, int32_t n, const vt_camera* cams,
                                   const vt_hit* const* d_hits, const vt_shade_inputs* in, const float* const* d_targets,
                                   float* d_loss, float* d_grad_palette, float* d_grad_albedo, float* d_grad_sun,

@@ -137,6 +137,7 @@ _SIGNATURES = {
     "vt_trace_rays": (_S, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, _P]),
     "vt_shade_forward": (_S, [_P, _P, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P, _P, _P]),
     "vt_shade_backward": (_S, [_P, _P, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P, _P, _P, _P, _P]),
+    "vt_shade_forward_views": (_S, [_P, _P, C.c_int32, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P]),
     "vt_shade_backward_views": (_S, [_P, _P, C.c_int32, C.POINTER(Camera_t), _P, C.POINTER(ShadeInputs_t), _P, _P,
                                      _P, _P, _P, _P]),
     "vt_brickmap_create": (_S, [_P, C.POINTER(_P)]),
@@ -641,6 +642,15 @@ class Shading:
             self.ctx.handle, self.world.handle, C.byref(cam), d_hits.ptr, C.byref(self.inputs), d_target.ptr,
             self.d_loss.ptr, self.d_gpal.ptr, self.d_galb.ptr if self.d_galb is not None else None,
             self.d_gsun.ptr, stream))
+
+    def forward_views(self, cams, d_hits, d_rgbs, stream=None) -> None:
+        """forward over many views in one call (concurrent internally)."""
+        n = len(cams)
+        cam_arr = (Camera_t * n)(*cams)
+        hits = (C.c_void_p * n)(*[h.ptr for h in d_hits])
+        rgbs = (C.c_void_p * n)(*[r.ptr for r in d_rgbs])
+        self.ctx.check(self.ctx.lib.vt_shade_forward_views(self.ctx.handle, self.world.handle, n, cam_arr, hits,
+                                                           C.byref(self.inputs), rgbs, stream))
 
     def backward_views(self, cams, d_hits, d_targets, stream=None) -> None:
         """backward over many views in one call (concurrent internally)."""
