@@ -12,9 +12,10 @@
 // the hit exactly as the render kernel does (same origin arithmetic, same
 // traversal), instead of being stored between passes.  The backward kernel is
 // the forward kernel plus the loss and gradient epilogue, one thread per
-// pixel.  Gradients are summed per warp over lanes that share a material or a
-// voxel (__match_any_sync groups), per block in shared memory, then once per
-// block with global atomics.
+// pixel.  Palette gradients are summed per warp over the lanes that share a
+// material (the warp walks its distinct materials), per block in shared
+// memory, then once per block with global atomics; albedo gradients go to
+// global memory with one atomic per pixel.
 #include <cstring>
 
 #include "shade.cuh"
@@ -45,18 +46,6 @@ struct AdjArgs {
     float* gsun;
 };
 
-// Sum of v over the lanes of group g (every lane of g gets the same value,
-// summed in lane order).
-__device__ __forceinline__ float group_sum(unsigned g, float v) {
-    float s = 0.0f;
-    unsigned mm = g;
-    while (mm) {
-        const int l = __ffs(mm) - 1;
-        s += __shfl_sync(g, v, l);
-        mm &= mm - 1u;
-    }
-    return s;
-}
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -158,22 +147,28 @@ __global__ void __launch_bounds__(kAdjBlock) k_shade(AdjArgs a) {
             for (int k = 0; k < 3; ++k) gs[k] = coef * (nrm[k] - ndl_raw * a.sun_n[k]);
         }
     }
-    // palette: one shared-memory atomic per (warp, material)
+    // palette: one shared-memory atomic per (warp, material).  The warp walks
+    // its distinct materials (few per warp) with butterfly sums, no
+    // divergence.
     {
-        const unsigned grp = __match_any_sync(0xFFFFFFFFu, hit ? m : -1);
-        const float s0 = group_sum(grp, gp[0]), s1 = group_sum(grp, gp[1]), s2 = group_sum(grp, gp[2]);
-        if (hit && lane == __ffs(grp) - 1) {
-            atomicAdd(s_gpal + 3 * m + 0, s0);
-            atomicAdd(s_gpal + 3 * m + 1, s1);
-            atomicAdd(s_gpal + 3 * m + 2, s2);
+        unsigned todo = __ballot_sync(0xFFFFFFFFu, hit);
+        while (todo) {
+            const int leader = __ffs(todo) - 1;
+            const int key = __shfl_sync(0xFFFFFFFFu, m, leader);
+            const bool mine = hit && m == key;
+            todo &= ~__ballot_sync(0xFFFFFFFFu, mine);
+            const float s0 = warp_sum(mine ? gp[0] : 0.0f), s1 = warp_sum(mine ? gp[1] : 0.0f),
+                        s2 = warp_sum(mine ? gp[2] : 0.0f);
+            if (lane == leader) {
+                atomicAdd(s_gpal + 3 * key + 0, s0);
+                atomicAdd(s_gpal + 3 * key + 1, s1);
+                atomicAdd(s_gpal + 3 * key + 2, s2);
+            }
         }
     }
-    // albedo: one global atomic per (warp, voxel)
-    if (a.galb) {
-        const unsigned grp = __match_any_sync(0xFFFFFFFFu, hit ? v : 0xFFFFFFFFu);
-        const float s = group_sum(grp, ga);
-        if (hit && lane == __ffs(grp) - 1) atomicAdd(a.galb + v, s);
-    }
+    // albedo: one global atomic per hit pixel (voxels differ across most of
+    // a warp; the L2 absorbs the few repeats)
+    if (a.galb && hit) atomicAdd(a.galb + v, ga);
     // loss and sun: warp sums, then shared memory
     {
         const float l = warp_sum(lossv), x = warp_sum(gs[0]), y = warp_sum(gs[1]), z = warp_sum(gs[2]);
