@@ -516,7 +516,25 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the config 2/3/4 measurements that follow the headline")
+    ap.add_argument("--only", choices=["config2", "config3", "config4"],
+                    help="run just one of the other configurations and print its result (for profiling)")
     args = ap.parse_args()
+    if args.only:
+        import torch
+        sys.path.insert(0, str(PKG))
+        _load("vt_build", PKG / "build.py").build()
+        import scenes
+        import vt
+        ctx = vt.Context(0)
+        if args.only == "config2":
+            res = measure_config2(vt, scenes, ctx, torch, torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda"))
+        elif args.only == "config3":
+            res = measure_config3(vt, scenes, ctx, torch)
+        else:
+            res = measure_config4(vt, scenes, ctx, torch)
+        print(json.dumps({"only": args.only, **res}), flush=True)
+        ctx.close()
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
