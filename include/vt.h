@@ -24,7 +24,8 @@
  *   - vt_sync() waits for a stream and surfaces the device status word that the
  *     checked kernels write (VT_ERR_DEVICE_OOB, VT_ERR_TIMEOUT).
  *   - One vt_ctx per host thread; the library holds no global mutable state
- *     besides CUDA's own.
+ *     besides CUDA's own and the fixed device array behind
+ *     vt_render_host_static.
  */
 #ifndef VT_H
 #define VT_H
