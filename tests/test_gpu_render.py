@@ -315,6 +315,12 @@ def test_deferred_bounce_pass_equals_inline(vt, ctx):
             assert np.array_equal(got, want)
             assert ((got["flags"] & vt.HIT_BOUNCE) != 0).sum() > 1000
             assert np.array_equal(vt.render_host(ctx, w, c, p), want)
+            pb = vt.PinnedBuffer(ctx, c.width * c.height, vt.HIT_DTYPE)   # kernels write host memory directly
+            try:
+                vt.render_host(ctx, w, c, p, pb.array)
+                assert np.array_equal(pb.array, want)
+            finally:
+                pb.free()
     finally:
         for b in bufs:
             b.free()
