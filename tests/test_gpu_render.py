@@ -2,7 +2,8 @@
 
 Bar: hit voxel, entry face, material, flags and t bit-exact; shaded RGBA8
 within 1/255 per channel (the only float code outside the traversal whose
-rounding may differ is powf in the vignette).
+rounding may differ is the vignette: the device multiplies a column and a row
+power, the oracle takes one powf of the product, as the reference does).
 """
 import numpy as np
 import pytest

@@ -54,14 +54,16 @@ __global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldVi
     using BT = BlockTile<TW>;
     // screen coordinates of the block's columns and rows, once per block
     // instead of four divisions per pixel
-    __shared__ float s_col[2][BT::kW], s_row[2][BT::kH];
+    __shared__ float s_col[3][BT::kW], s_row[3][BT::kH];
     const int x0 = blockIdx.x * BT::kW, y0 = f.row0 + blockIdx.y * BT::kH;
     if (threadIdx.x < BT::kW) {
         s_col[0][threadIdx.x] = ray_u(f, x0 + (int)threadIdx.x);
         s_col[1][threadIdx.x] = centre_u(f, x0 + (int)threadIdx.x);
+        s_col[2][threadIdx.x] = vignette_u(s_col[1][threadIdx.x]);
     } else if (threadIdx.x >= 64 && threadIdx.x < 64 + BT::kH) {
         s_row[0][threadIdx.x - 64] = ray_v(f, y0 + (int)threadIdx.x - 64);
         s_row[1][threadIdx.x - 64] = centre_v(f, y0 + (int)threadIdx.x - 64);
+        s_row[2][threadIdx.x - 64] = vignette_v(s_row[1][threadIdx.x - 64]);
     }
     if (SMEM)
         for (unsigned i = threadIdx.x; i < w.ncoarse; i += blockDim.x) s_coarse[i] = __ldg(w.coarse + i);
@@ -78,6 +80,8 @@ __global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldVi
         uv.cu = s_col[1][lx];
         uv.rv = s_row[0][ly];
         uv.cv = s_row[1][ly];
+        uv.gu = s_col[2][lx];
+        uv.gv = s_row[2][ly];
         uint4 rec;
         if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, w.cdist, f, px, py, uv, status, pc);
         else rec = render_pixel<STATS, CHECKED>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, uv, status, pc);

@@ -70,7 +70,7 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
         bool shadowed = false;
         if (f.rays & VT_RAYS_SHADOW) {
             PRay rs;
-            pray_init(rs, so, f.sun);
+            pray_init_dir(rs, so, f.sun_d, f.sun_inv);
             TraceHit hs;
             shadowed = trace_any<STATS, CHECKED, false, true>(w, coarse, cd, rs, f.shadow_max_steps, hs, cnt, status);
             if (shadowed) flags |= VT_HIT_SHADOWED;

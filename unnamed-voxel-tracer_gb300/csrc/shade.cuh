@@ -31,6 +31,9 @@ struct FrameParams {
     float sun_n[3];     // normalised sun direction
     float lit_sky[3];   // SkyDome2 of the RGBA8-stored sun direction (blit.fragment.glsl:31)
     float lit_a;        // illumination alpha 0.3 stored in RGBA8
+    float sun_d[3];     // the shadow rays' direction as traced (a zero component made 0.001, map.glsl:85-90)
+    float sun_inv[3];   // its correctly rounded reciprocal
+    float cross_r2;     // the largest x with sqrt(x) <= 0.002 (crosshair radius test without a square root)
     int row0, row_end;  // rows [row0, row_end) of the image this launch renders
     void* bounce_jobs;       // non-null: bounce rays are queued here (BounceJob), not traced inline
     unsigned* bounce_count;  // the queue's length
@@ -41,6 +44,7 @@ struct FrameParams {
 struct PixelUV {
     float ru, rv;  // the primary ray's UV (primary.comp.glsl:31-36)
     float cu, cv;  // the pixel centre in [0, 1] (vignette, crosshair)
+    float gu, gv;  // the vignette's column and row factors
 };
 
 __device__ __forceinline__ float ray_u(const FrameParams& f, int px) {
@@ -58,12 +62,21 @@ __device__ __forceinline__ float ray_v(const FrameParams& f, int py) {
 __device__ __forceinline__ float centre_u(const FrameParams& f, int px) { return ((float)px + 0.5f) / (float)f.width; }
 __device__ __forceinline__ float centre_v(const FrameParams& f, int py) { return ((float)py + 0.5f) / (float)f.height; }
 
+// The vignette pow(15 u (1 - u) v (1 - v), 0.18) (blit.fragment.glsl:15-21,34)
+// as the product of a column factor pow(15 u (1 - u), 0.18) and a row factor
+// pow(v (1 - v), 0.18), so that a block computes the powers once per column
+// and row.  The product is within a few ulp of the joint power.
+__device__ __forceinline__ float vignette_u(float u) { return powf(15.0f * (u * (1.0f - u)), 0.18f); }
+__device__ __forceinline__ float vignette_v(float v) { return powf(v * (1.0f - v), 0.18f); }
+
 __device__ __forceinline__ PixelUV pixel_uv(const FrameParams& f, int px, int py) {
     PixelUV uv;
     uv.ru = ray_u(f, px);
     uv.rv = ray_v(f, py);
     uv.cu = centre_u(f, px);
     uv.cv = centre_v(f, py);
+    uv.gu = vignette_u(uv.cu);
+    uv.gv = vignette_v(uv.cv);
     return uv;
 }
 
@@ -151,15 +164,9 @@ __device__ __forceinline__ void sky_n(const float sn[3], const float rd[3], floa
     col[2] = ((0.75f - dy * 1.0f) + (0.15f * 0.5f)) + (0.4f * 0.1f) * s8 + 0.04f * s3;
 }
 
-// u, v: the pixel centre in [0, 1] (PixelUV::cu, cv)
-__device__ __forceinline__ float vignette(float u, float v) {
-    const float a = u * (1.0f - u), b = v * (1.0f - v);
-    return powf(a * b * 15.0f, 0.18f);
-}
-
-__device__ __forceinline__ bool crosshair(float cu, float cv) {
+__device__ __forceinline__ bool crosshair(const FrameParams& f, float cu, float cv) {
     const float u = cu - 0.5f, v = cv - 0.5f;
-    return __fsqrt_rn(u * u + v * v) <= 0.002f;
+    return u * u + v * v <= f.cross_r2;
 }
 
 __device__ __forceinline__ unsigned wang_hash(unsigned& seed) {
@@ -272,14 +279,14 @@ __device__ __forceinline__ void shade_miss(const FrameParams& f, const float d[3
 
 __device__ __forceinline__ unsigned composite_uv(const FrameParams& f, const PixelUV& uv, float col[4]) {
     if (f.shade == VT_SHADE_REFERENCE) {
-        if ((f.flags & VT_FLAG_CROSSHAIR) && crosshair(uv.cu, uv.cv)) {
+        if ((f.flags & VT_FLAG_CROSSHAIR) && crosshair(f, uv.cu, uv.cv)) {
             col[0] = col[0] * 0.5f + 0.5f;
             col[1] = col[1] * 0.5f + 0.5f;
             col[2] = col[2] * 0.5f + 0.5f;
             col[3] = col[3] * 0.5f + 0.2f;
         }
         if (f.flags & VT_FLAG_VIGNETTE) {
-            const float g = vignette(uv.cu, uv.cv);
+            const float g = uv.gu * uv.gv;
 #pragma unroll
             for (int j = 0; j < 4; ++j) col[j] = g * col[j];
         }
@@ -301,6 +308,16 @@ inline void frame_constants(FrameParams& f) {
     for (int j = 0; j < 3; ++j) sq[j] = (float)unorm8(f.sun[j]) / 255.0f;
     sky(f.sun, sq, f.lit_sky);
     f.lit_a = (float)unorm8(0.3f) / 255.0f;
+    for (int j = 0; j < 3; ++j) {
+        f.sun_d[j] = f.sun[j] == 0.0f ? 0.001f : f.sun[j];
+        f.sun_inv[j] = 1.0f / f.sun_d[j];
+    }
+    // square roots round monotonically: sqrt(x) <= r iff x <= the largest such x
+    const float r = 0.002f;
+    float x = r * r;
+    while (sqrtf(x) > r) x = nextafterf(x, 0.0f);
+    while (sqrtf(nextafterf(x, INFINITY)) <= r) x = nextafterf(x, INFINITY);
+    f.cross_r2 = x;
 }
 
 }  // namespace vt

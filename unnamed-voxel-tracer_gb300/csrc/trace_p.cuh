@@ -46,6 +46,19 @@ __device__ __forceinline__ void pray_init(PRay& r, const float o[3], const float
     }
 }
 
+// pray_init with a direction whose zero components are already replaced and
+// whose reciprocal is given (the shadow rays of a frame share both).
+__device__ __forceinline__ void pray_init_dir(PRay& r, const float o[3], const float d[3], const float inv[3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        r.o[i] = o[i];
+        r.d[i] = d[i];
+        r.inv[i] = inv[i];
+        r.oinv[i] = -__fmul_rn(o[i], inv[i]);
+        r.pos[i] = d[i] > 0.0f;
+    }
+}
+
 // Whether a ray origin is near enough for the one-correction plane search
 // (advance_axis<true>).
 __host__ __device__ __forceinline__ bool near_origin(const float o[3]) {
@@ -361,32 +374,32 @@ struct Walker {
     __device__ __forceinline__ int step(const WorldView& w, const unsigned char* cdist, TraceHit& h) {
         bool jump = false;
         int sh = 0, rad = 0;
-        if (state == 0) {
+        if (state != 2) {
+            // the current cell and its chunk (nk is exact in states 0 and 1)
 #pragma unroll
             for (int i = 0; i < 3; ++i) c[i] = r.pos[i] ? nk[i] - 1 : nk[i];
             const unsigned ci = (unsigned)(c[0] >> 5) + (unsigned)w.cdim[0] * ((unsigned)(c[1] >> 5) + (unsigned)w.cdim[1] * (unsigned)(c[2] >> 5));
-            const int dc = cdist[oct * w.cstride + ci];
-            if (dc) {
-                jump = true;
-                sh = 5;
-                rad = dc;
-            } else {
-                state = 1;
+            if (state == 0) {
+                const int dc = cdist[oct * w.cstride + ci];
+                if (dc) {
+                    jump = true;
+                    sh = 5;
+                    rad = dc;
+                } else {
+                    state = 1;
+                }
             }
-        }
-        if (state == 1) {
-#pragma unroll
-            for (int i = 0; i < 3; ++i) c[i] = r.pos[i] ? nk[i] - 1 : nk[i];
-            const unsigned ci = (unsigned)(c[0] >> 5) + (unsigned)w.cdim[0] * ((unsigned)(c[1] >> 5) + (unsigned)w.cdim[1] * (unsigned)(c[2] >> 5));
-            wi = ci * 512u + ((unsigned)((c[0] >> 2) & 7) | ((unsigned)((c[1] >> 2) & 7) << 3) | ((unsigned)((c[2] >> 2) & 7) << 6));
-            word = __ldg(w.mask + wi);
-            if (word == 0ull) {
-                jump = true;
-                sh = 2;
-                rad = __ldg(w.bdist + (size_t)oct * w.nwords + wi);
-            } else {
-                vb = (unsigned)(c[0] & 3) | ((unsigned)(c[1] & 3) << 2) | ((unsigned)(c[2] & 3) << 4);
-                state = 2;
+            if (state == 1) {
+                wi = ci * 512u + ((unsigned)((c[0] >> 2) & 7) | ((unsigned)((c[1] >> 2) & 7) << 3) | ((unsigned)((c[2] >> 2) & 7) << 6));
+                word = __ldg(w.mask + wi);
+                if (word == 0ull) {
+                    jump = true;
+                    sh = 2;
+                    rad = __ldg(w.bdist + (size_t)oct * w.nwords + wi);
+                } else {
+                    vb = (unsigned)(c[0] & 3) | ((unsigned)(c[1] & 3) << 2) | ((unsigned)(c[2] & 3) << 4);
+                    state = 2;
+                }
             }
         }
         if (!jump) {
@@ -443,7 +456,8 @@ struct Walker {
             const int u = c[i] >> sh;
             // a brick distance d promises d-1 bricks ahead across and
             // (d-1)/kFlatY vertically (kFlatY-weighted Chebyshev distance)
-            const int ri = (i == 1 && sh == 2) ? (rad - 1) / kFlatY + 1 : rad;
+            // (rad >= 1 in an empty unit: an unsigned quotient, a shift)
+            const int ri = (i == 1 && sh == 2) ? (int)((unsigned)(rad - 1) / (unsigned)kFlatY) + 1 : rad;
             K[i] = r.pos[i] ? (u + ri) * (1 << sh) : (u - (ri - 1)) * (1 << sh);
             tK[i] = ptime(r, i, K[i]);
         }
