@@ -33,6 +33,12 @@ vt_status take_status(vt_ctx* ctx, unsigned st) {
     return fail(ctx, VT_ERR_TIMEOUT, "a bounded device wait gave up");
 }
 
+vt_status note_status_writer(vt_ctx* ctx, cudaStream_t st) {
+    ctx->status_dirty = true;
+    VT_CUDA(ctx, cudaEventRecord(ctx->ev_status, st));
+    return VT_OK;
+}
+
 vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out) {
     if (bytes > ctx->scratch_bytes) {
         if (ctx->d_scratch) {
@@ -94,6 +100,7 @@ vt_status vt_ctx_create(int32_t device, vt_ctx** out) {
         if ((e = cudaMalloc(&ctx->d_work, kWorkSlots * sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
         if ((e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_status), sizeof(unsigned), cudaHostAllocDefault)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaHostAlloc"); break; }
         *ctx->h_status = 0;
+        if ((e = cudaEventCreateWithFlags(&ctx->ev_status, cudaEventDisableTiming)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaEventCreate"); break; }
         // blocking stream: *_host calls order after work queued on the legacy default stream
         if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamDefault)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaStreamCreate"); break; }
     } while (0);
@@ -118,6 +125,7 @@ vt_status vt_ctx_destroy(vt_ctx* ctx) {
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    if (ctx->ev_status) cudaEventDestroy(ctx->ev_status);
     if (ctx->d_bounce_jobs) cudaFree(ctx->d_bounce_jobs);
     if (ctx->d_bounce_open) cudaFree(ctx->d_bounce_open);
     if (ctx->d_bounce_ctr) cudaFree(ctx->d_bounce_ctr);
@@ -137,10 +145,25 @@ const char* vt_last_error_string(const vt_ctx* ctx) { return ctx ? ctx->last_err
 
 vt_status vt_sync(vt_ctx* ctx, vt_stream stream) {
     if (!ctx) return VT_ERR_ARG;
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (!ctx->status_dirty) {
+        // no launch since the last read can have set the word
+        VT_CUDA(ctx, cudaStreamSynchronize(st));
+        return VT_OK;
+    }
+    // the read sees every status-setting launch so far if they were all done
+    // before it was issued; only then is the word clean afterwards
+    const cudaError_t q = cudaEventQuery(ctx->ev_status);
+    if (q == cudaErrorNotReady) {
+        const cudaError_t le = cudaGetLastError();  // a pending query result is no error
+        if (le != cudaSuccess && le != cudaErrorNotReady) return check_cuda(ctx, le, "cudaEventQuery");
+    } else if (q != cudaSuccess) {
+        return check_cuda(ctx, q, "cudaEventQuery");
+    }
     // the status word travels on the same stream: one synchronisation
-    VT_CUDA(ctx, cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost,
-                                 (cudaStream_t)stream));
-    VT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+    VT_CUDA(ctx, cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    VT_CUDA(ctx, cudaStreamSynchronize(st));
+    if (q == cudaSuccess) ctx->status_dirty = false;
     return take_status(ctx, *ctx->h_status);
 }
 

@@ -406,6 +406,7 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
 #undef VT_LAUNCH_M
 #undef VT_LAUNCH
     VT_CUDA(ctx, cudaGetLastError());
+    if (stats || checked) return note_status_writer(ctx, stream);  // the model walk checks its indexes
     if (defer) return launch_bounce(ctx, world, f, d_out, stream);
     return VT_OK;
 }
@@ -552,7 +553,7 @@ vt_status vt_trace_rays(vt_ctx* ctx, const vt_world* world, const float* d_origi
     k_trace_rays<true><<<(n + kBlock - 1) / kBlock, kBlock, 0, (cudaStream_t)stream>>>(
         w, d_origins, d_dirs, n, max_steps, reinterpret_cast<uint4*>(d_out), ctx->d_status);
     VT_CUDA(ctx, cudaGetLastError());
-    return VT_OK;
+    return note_status_writer(ctx, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -87,6 +87,10 @@ struct vt_ctx {
     cudaEvent_t ev_start = nullptr;
     cudaEvent_t ev_band[16] = {};
     unsigned* h_status = nullptr;  // pinned copy of d_status
+    // launches that may set d_status (checked and instrumented kernels) mark
+    // it dirty and record ev_status; while it is clean vt_sync need not read it
+    bool status_dirty = false;
+    cudaEvent_t ev_status = nullptr;
     // the deferred bounce pass (bounce.cu): ray queue, results, counters
     void* d_bounce_jobs = nullptr;
     unsigned char* d_bounce_open = nullptr;
@@ -156,6 +160,8 @@ vt_status check_cuda(vt_ctx* ctx, cudaError_t err, const char* what);
 // Turns a device status word read back by the caller into the call's status
 // (clearing the device word when it was set).
 vt_status take_status(vt_ctx* ctx, unsigned st);
+// Marks the status word as possibly set by a launch just queued on st.
+vt_status note_status_writer(vt_ctx* ctx, cudaStream_t st);
 // Context-owned device buffer of at least `bytes` (grown on demand).
 vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out);
 // Rebuilds the empty-space distances of a world on `st`.
