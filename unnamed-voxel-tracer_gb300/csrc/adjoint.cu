@@ -195,7 +195,7 @@ vt_status launch_shade(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
     if (!ctx) return VT_ERR_ARG;
     if (!world || !cam || !d_hits || !in || !in->d_palette) return fail(ctx, VT_ERR_ARG, "null shading argument");
     if (world->ctx != ctx) return fail(ctx, VT_ERR_ARG, "world belongs to another context");
-    if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
+    if (cam->width <= 0 || cam->height <= 0 || cam->width > kMaxImageSide || cam->height > kMaxImageSide)
         return fail(ctx, VT_ERR_ARG, "camera size out of range (1..32768)");
     const float len2 = (in->sun[0] * in->sun[0] + in->sun[1] * in->sun[1]) + in->sun[2] * in->sun[2];
     if (!(len2 > 0.0f)) return fail(ctx, VT_ERR_ARG, "sun direction must be nonzero");

@@ -525,7 +525,7 @@ vt_status vt_render_reference(vt_ctx* ctx, const vt_brickmap* bm, const vt_camer
                               vt_stream stream) {
     if (!ctx) return VT_ERR_ARG;
     if (!bm || !cam || !d_out) return fail(ctx, VT_ERR_ARG, "null brickmap, camera or output");
-    if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
+    if (cam->width <= 0 || cam->height <= 0 || cam->width > kMaxImageSide || cam->height > kMaxImageSide)
         return fail(ctx, VT_ERR_ARG, "camera size out of range (1..32768)");
     RefFrame f;
     for (int i = 0; i < 4; ++i) f.pos[i] = cam->pos[i];

@@ -310,7 +310,7 @@ vt_status check_frame_args(vt_ctx* ctx, const vt_world* world, const vt_camera* 
     if (!ctx) return VT_ERR_ARG;
     if (!world || !cam || !p) return fail(ctx, VT_ERR_ARG, "null world, camera or params");
     if (world->ctx != ctx) return fail(ctx, VT_ERR_ARG, "world belongs to another context");
-    if (cam->width <= 0 || cam->height <= 0 || cam->width > 32768 || cam->height > 32768)
+    if (cam->width <= 0 || cam->height <= 0 || cam->width > kMaxImageSide || cam->height > kMaxImageSide)
         return fail(ctx, VT_ERR_ARG, "camera size out of range (1..32768)");
     if (p->shade > VT_SHADE_LAMBERT) return fail(ctx, VT_ERR_ARG, "unknown shade mode");
     return VT_OK;

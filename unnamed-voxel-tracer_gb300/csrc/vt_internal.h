@@ -62,6 +62,8 @@ __host__ __device__ inline unsigned cdist_stride(unsigned nchunks) { return (nch
 constexpr int kFlatY = 4;
 // Capacity of a world's entity box list.
 constexpr int kMaxEntities = 1024;
+// Largest image width and height a frame may have.
+constexpr int kMaxImageSide = 32768;
 
 }  // namespace vt
 
@@ -97,6 +99,7 @@ struct vt_ctx {
     unsigned* d_bounce_ctr = nullptr;  // {queued, taken}
     size_t bounce_capacity = 0;
     cudaEvent_t ev_bounce = nullptr;   // the last deferred frame is done with the queue
+    void* d_screen = nullptr;          // per-column and per-row composite coordinates (float2 each)
     int bounce_blocks = 0;
 };
 
