@@ -496,6 +496,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         "rays_per_step": job_rays / args.steps,
         "per_ray": {k: sum(s[k] for s in stats) / sum(rays) for k in ("steps", "iterations", "mask_words",
                                                                        "coarse_words")},
+        # unit crossings per second (a jump over an empty box counts every crossing it skips)
+        "steps_per_s": value * 1e9 * sum(s["steps"] for s in stats) / sum(rays),
         "e2e": {"value": e2e_value, "unit": "Grays/s", "h2d_bytes_per_step": C.sizeof(vt.Camera_t) + C.sizeof(vt.Params_t),
                 "d2h_bytes_per_step": nbytes,
                 "note": "vt_render_host into pinned host memory: camera and params travel in the launch; the kernel writes the records across the host link"},
