@@ -385,14 +385,14 @@ vt_status vt_shade_backward(vt_ctx* ctx, const vt_world* world, const vt_camera*
                             const vt_shade_inputs* in, const float* d_target, float* d_loss, float* d_grad_palette,
                             float* d_grad_albedo, float* d_grad_sun, vt_stream stream);
 /* vt_shade_forward over n views (cameras, hit records, output images; the
- * shadow term traced), as one call: the views run concurrently on the
- * context's internal streams, forked from and joined back into `stream`. */
+ * shadow term traced), as one call: up to 16 views share one launch on
+ * `stream`; views may differ in size. */
 vt_status vt_shade_forward_views(vt_ctx* ctx, const vt_world* world, int32_t n, const vt_camera* cams,
                                  const vt_hit* const* d_hits, const vt_shade_inputs* in, float* const* d_rgb,
                                  vt_stream stream);
 /* vt_shade_backward over n views (cameras, hit records, targets) into the
- * same accumulators, as one call: the views run concurrently on the
- * context's internal streams, forked from and joined back into `stream`. */
+ * same accumulators, as one call: up to 16 views share one launch on
+ * `stream`; views may differ in size. */
 vt_status vt_shade_backward_views(vt_ctx* ctx, const vt_world* world, int32_t n, const vt_camera* cams,
                                   const vt_hit* const* d_hits, const vt_shade_inputs* in, const float* const* d_targets,
                                   float* d_loss, float* d_grad_palette, float* d_grad_albedo, float* d_grad_sun,

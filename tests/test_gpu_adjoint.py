@@ -171,3 +171,51 @@ def test_forward_views_equals_per_view_calls(vt, ctx, scene):
         assert np.array_equal(a.download(np.zeros(n * 3, np.float32)), b.download(np.zeros(n * 3, np.float32)))
     for b in one + many:
         b.free()
+
+
+def test_views_of_mixed_sizes_beyond_one_launch(vt, ctx, scene):
+    """18 views of five sizes (two launches of the multi-view kernel, views
+    smaller than its grid): forward images equal the per-view calls, loss and
+    gradients agree up to the order of the float atomics."""
+    s = scene
+    d = vt.gen_desc((256, 256, 256), seed=4, trees=50)
+    sizes = [(128, 96), (64, 40), (17, 9), (1, 1), (100, 3)]
+    cams = [vt.gen_camera(d, v % 3, *sizes[v % len(sizes)]) for v in range(18)]
+    prim = vt.default_params(rays=vt.RAYS_PRIMARY, shade=vt.SHADE_NONE)
+    rng = np.random.default_rng(7)
+    hits, tgts, one, many = [], [], [], []
+    for cam in cams:
+        n = cam.width * cam.height
+        hb = ctx.alloc(n * 16)
+        vt.render(ctx, s["world"], cam, prim, hb)
+        hits.append(hb)
+        dt = ctx.alloc(n * 12)
+        dt.upload(rng.uniform(0, 1, (n, 3)).astype(np.float32))
+        tgts.append(dt)
+        one.append(ctx.alloc(n * 12))
+        many.append(ctx.alloc(n * 12))
+    ctx.sync()
+    sh = s["sh"]
+    for cam, hb, rb in zip(cams, hits, one):
+        sh.forward(cam, hb, rb)
+    sh.forward_views(cams, hits, many)
+    ctx.sync()
+    for cam, a, b in zip(cams, one, many):
+        n = cam.width * cam.height
+        assert np.array_equal(a.download(np.zeros(n * 3, np.float32)), b.download(np.zeros(n * 3, np.float32)))
+    sh.zero_grad()
+    for cam, hb, dt in zip(cams, hits, tgts):
+        sh.backward(cam, hb, dt)
+    g1 = sh.grads()
+    sh.zero_grad()
+    sh.backward_views(cams, hits, tgts)
+    g2 = sh.grads()
+    for k in ("palette", "sun"):
+        scale = np.abs(g1[k]).max()
+        assert scale > 0 and np.abs(g2[k] - g1[k]).max() <= 1e-5 * scale, k
+    assert abs(g2["loss"] - g1["loss"]) <= 1e-5 * abs(g1["loss"])
+    if "albedo" in g1:
+        scale = np.abs(g1["albedo"]).max()
+        assert np.abs(g2["albedo"] - g1["albedo"]).max() <= 1e-5 * scale
+    for b in hits + tgts + one + many:
+        b.free()
