@@ -454,8 +454,8 @@ vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* ca
     const size_t bytes = W * H * sizeof(vt_hit);
     // Pinned host memory is mapped into the device's address space: the
     // kernel stores the records straight into it over the host link, with no
-    // staging copy (1080p: 274 us per frame end to end against 309 us for the
-    // band pipeline below, kernel alone 234 us).
+    // staging copy (1080p: 244 us per frame end to end against 288 us for the
+    // band pipeline below, kernel alone 210 us).
     {
         cudaPointerAttributes pa;
         if (cudaPointerGetAttributes(&pa, h_out) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {
