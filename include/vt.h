@@ -203,7 +203,11 @@ void vt_params_default(vt_params* p);
 /* Game.render (game.zig:232-256): primary rays, optional shadow and bounce
  * rays and the shading of primary.comp + secondary.comp + blit.fragment, fused
  * into one launch.  d_out holds width*height records, row-major, row 0 at
- * v = -1 (bottom of the image, as the GL image is addressed). */
+ * v = -1 (bottom of the image, as the GL image is addressed).
+ * The first frame of a new image size and field of view in a context makes
+ * that frame's table of per-column and per-row screen coordinates (one small
+ * device allocation and one synchronisation of `stream`; up to 8 tables per
+ * context, none inside a graph capture). */
 vt_status vt_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam,
                     const vt_params* params, vt_hit* d_out, vt_stream stream);
 /* Same, with host output, synchronous.  Into pinned memory (vt_host_alloc_

@@ -47,3 +47,35 @@ def test_batch_matches_per_job_renders(vt, ctx, oracle, kernel):
         buf.free()
     for w in worlds:
         w.close()
+
+
+def test_batch_captured_in_a_fresh_context(vt):
+    """A context that has rendered nothing yet holds no screen tables: the
+    batch graph is captured without making any (no allocation or
+    synchronisation inside a capture) and still equals the per-job renders,
+    which then make the tables."""
+    ctx = vt.Context(0)
+    try:
+        d = vt.gen_desc((96, 64, 80), scale=0.5, seed=77)
+        w = vt.World(ctx, (96, 64, 80))
+        w.upload_dense(vt.gen_world(d))
+        params = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=vt.gen_sun(77))
+        jobs = []
+        for c, (W, H) in enumerate([(70, 41), (128, 72), (70, 41)]):
+            cam = vt.gen_camera(d, c, W, H)
+            jobs.append((w, cam, ctx.alloc(W * H * 16)))
+        batch = vt.Batch(ctx, jobs, params)
+        batch.launch()
+        ctx.sync()
+        for i, (_, cam, buf) in enumerate(jobs):
+            got = buf.download(np.zeros(cam.width * cam.height, vt.HIT_DTYPE))
+            if i == 0:  # the allocation-free entry point before any table of this size exists
+                assert np.array_equal(got, vt.render_host_static(ctx, w, cam, params))
+            assert np.array_equal(got, vt.render_host(ctx, w, cam, params))
+            assert np.array_equal(got, vt.render_host_static(ctx, w, cam, params))
+        batch.close()
+        for _, _, buf in jobs:
+            buf.free()
+        w.close()
+    finally:
+        ctx.close()

@@ -130,7 +130,7 @@ vt_status vt_ctx_destroy(vt_ctx* ctx) {
     if (ctx->d_bounce_open) cudaFree(ctx->d_bounce_open);
     if (ctx->d_bounce_ctr) cudaFree(ctx->d_bounce_ctr);
     if (ctx->ev_bounce) cudaEventDestroy(ctx->ev_bounce);
-    if (ctx->d_screen) cudaFree(ctx->d_screen);
+    for (int i = 0; i < ctx->n_screen; ++i) cudaFree(ctx->screen[i].d);
     for (int i = 0; i < kMaxBands; ++i)
         if (ctx->ev_band[i]) cudaEventDestroy(ctx->ev_band[i]);
     if (ctx->d_scratch) cudaFree(ctx->d_scratch);

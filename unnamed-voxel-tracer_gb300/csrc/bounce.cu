@@ -57,42 +57,19 @@ __global__ void __launch_bounds__(kBounceBlock) k_bounce_trace(WorldView w, cons
     }
 }
 
-// The composite's screen coordinates of every column (pixel centre u and the
-// vignette's column factor) and row (v and the row factor), so that the finish
-// kernel reads them instead of dividing and taking powers per pixel.
-__global__ void __launch_bounds__(kBounceBlock) k_screen_tables(FrameParams f, float2* __restrict__ cols,
-                                                                float2* __restrict__ rows) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < f.width) {
-        const float cu = centre_u(f, i);
-        cols[i] = make_float2(cu, vignette_u(cu));
-    } else if (i < f.width + f.height) {
-        const float cv = centre_v(f, i - f.width);
-        rows[i - f.width] = make_float2(cv, vignette_v(cv));
-    }
-}
-
 // One thread per deferred pixel: the shading render_pixel would have done with
 // this bounce result, and the record's rgba and VT_HIT_BOUNCE flag.
 __global__ void __launch_bounds__(kBounceBlock) k_bounce_finish(WorldView w, FrameParams f,
                                                                 const BounceJob* __restrict__ jobs,
                                                                 const unsigned* __restrict__ counters,
                                                                 const unsigned char* __restrict__ open,
-                                                                const float2* __restrict__ cols,
-                                                                const float2* __restrict__ rows,
                                                                 uint4* __restrict__ out) {
     const unsigned total = counters[0];
     for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x) {
         const BounceJob J = jobs[j];
         const unsigned p = J.pixel;
         const int px = (int)(p % (unsigned)f.width), py = (int)(p / (unsigned)f.width);
-        PixelUV uv;
-        const float2 cu = __ldg(cols + px), cv = __ldg(rows + py);
-        uv.ru = uv.rv = 0.0f;  // the primary ray is not needed here
-        uv.cu = cu.x;
-        uv.gu = cu.y;
-        uv.cv = cv.x;
-        uv.gv = cv.y;
+        const PixelUV uv = f.screen ? table_uv(f, px, py) : pixel_uv(f, px, py);
         uint4 r = out[p];
         const unsigned face = r.w & 0xFFu, mat = (r.w >> 8) & 0xFFu;
         unsigned flags = (r.w >> 16) & 0xFFu;
@@ -122,7 +99,6 @@ vt_status bounce_buffers(vt_ctx* ctx, size_t pixels) {
     VT_CUDA(ctx, cudaMalloc(&ctx->d_bounce_open, pixels));
     if (!ctx->d_bounce_ctr) VT_CUDA(ctx, cudaMalloc(&ctx->d_bounce_ctr, 2 * sizeof(unsigned)));
     if (!ctx->ev_bounce) VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_bounce, cudaEventDisableTiming));
-    if (!ctx->d_screen) VT_CUDA(ctx, cudaMalloc(&ctx->d_screen, 2 * kMaxImageSide * sizeof(float2)));
     ctx->bounce_capacity = pixels;
     return VT_OK;
 }
@@ -138,12 +114,8 @@ vt_status launch_bounce(vt_ctx* ctx, const vt_world* world, const FrameParams& f
     k_bounce_trace<<<ctx->bounce_blocks, kBounceBlock, 0, st>>>(w, jobs, ctx->d_bounce_ctr, ctx->d_bounce_ctr + 1,
                                                                 ctx->d_bounce_open, f.bounce_max_steps);
     VT_CUDA(ctx, cudaGetLastError());
-    float2* cols = reinterpret_cast<float2*>(ctx->d_screen);
-    float2* rows = cols + kMaxImageSide;
-    k_screen_tables<<<(f.width + f.height + kBounceBlock - 1) / kBounceBlock, kBounceBlock, 0, st>>>(f, cols, rows);
-    VT_CUDA(ctx, cudaGetLastError());
     k_bounce_finish<<<ctx->sm_count * 8, kBounceBlock, 0, st>>>(w, f, jobs, ctx->d_bounce_ctr, ctx->d_bounce_open,
-                                                                cols, rows, d_out);
+                                                                d_out);
     VT_CUDA(ctx, cudaGetLastError());
     // the next deferred frame of this context reuses the queue after this one
     VT_CUDA(ctx, cudaEventRecord(ctx->ev_bounce, st));

@@ -56,18 +56,19 @@ __global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldVi
     // instead of four divisions per pixel
     __shared__ float s_col[3][BT::kW], s_row[3][BT::kH];
     const int x0 = blockIdx.x * BT::kW, y0 = f.row0 + blockIdx.y * BT::kH;
-    if (threadIdx.x < BT::kW) {
+    const bool table = f.screen != nullptr;  // uniform: the frame's screen table replaces the block's
+    if (!table && threadIdx.x < BT::kW) {
         s_col[0][threadIdx.x] = ray_u(f, x0 + (int)threadIdx.x);
         s_col[1][threadIdx.x] = centre_u(f, x0 + (int)threadIdx.x);
         s_col[2][threadIdx.x] = vignette_u(s_col[1][threadIdx.x]);
-    } else if (threadIdx.x >= 64 && threadIdx.x < 64 + BT::kH) {
+    } else if (!table && threadIdx.x >= 64 && threadIdx.x < 64 + BT::kH) {
         s_row[0][threadIdx.x - 64] = ray_v(f, y0 + (int)threadIdx.x - 64);
         s_row[1][threadIdx.x - 64] = centre_v(f, y0 + (int)threadIdx.x - 64);
         s_row[2][threadIdx.x - 64] = vignette_v(s_row[1][threadIdx.x - 64]);
     }
     if (SMEM)
         for (unsigned i = threadIdx.x; i < w.ncoarse; i += blockDim.x) s_coarse[i] = __ldg(w.coarse + i);
-    __syncthreads();
+    if (SMEM || !table) __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int lx = (warp % BT::kWarpsX) * TW + (lane % TW), ly = (warp / BT::kWarpsX) * (32 / TW) + (lane / TW);
     const int px = x0 + lx, py = y0 + ly;
@@ -76,12 +77,16 @@ __global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldVi
     for (int k = 0; k < kNumCounters; ++k) pc.v[k] = 0;
     if (px < f.width && py < f.row_end) {
         PixelUV uv;
-        uv.ru = s_col[0][lx];
-        uv.cu = s_col[1][lx];
-        uv.rv = s_row[0][ly];
-        uv.cv = s_row[1][ly];
-        uv.gu = s_col[2][lx];
-        uv.gv = s_row[2][ly];
+        if (table) {
+            uv = table_uv(f, px, py);
+        } else {
+            uv.ru = s_col[0][lx];
+            uv.cu = s_col[1][lx];
+            uv.rv = s_row[0][ly];
+            uv.cv = s_row[1][ly];
+            uv.gu = s_col[2][lx];
+            uv.gv = s_row[2][ly];
+        }
         uint4 rec;
         if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, w.cdist, f, px, py, uv, status, pc);
         else rec = render_pixel<STATS, CHECKED>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, uv, status, pc);
@@ -292,6 +297,7 @@ FrameParams make_frame(const vt_camera* cam, const vt_params* p) {
     f.row_end = cam->height;
     f.bounce_jobs = nullptr;
     f.bounce_count = nullptr;
+    f.screen = nullptr;
     f.max_steps = p->max_steps;
     f.shadow_max_steps = p->shadow_max_steps;
     f.bounce_max_steps = p->bounce_max_steps;
@@ -335,8 +341,62 @@ vt_status band_streams(vt_ctx* ctx) {
     return VT_OK;
 }
 
+__global__ void __launch_bounds__(kBlock) k_screen_table(FrameParams f, float4* __restrict__ tab) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < f.width) {
+        const float cu = centre_u(f, i);
+        tab[i] = make_float4(ray_u(f, i), cu, vignette_u(cu), 0.0f);
+    } else if (i < f.width + f.height) {
+        const int y = i - f.width;
+        const float cv = centre_v(f, y);
+        tab[i] = make_float4(ray_v(f, y), cv, vignette_v(cv), 0.0f);
+    }
+}
+
+// The context's screen table for the frame's size and field of view, made on
+// first use (then synchronised once, so that frames on any stream may read
+// it).  Null, and the kernel computes the coordinates per block, when the
+// context already holds kScreenTables of them, when `create` is false (the
+// allocation-free entry point) or when `st` is being captured into a graph
+// (no allocation or synchronisation there).
+vt_status screen_table(vt_ctx* ctx, const FrameParams& f, cudaStream_t st, bool create, const float4** out) {
+    *out = nullptr;
+    for (int i = 0; i < ctx->n_screen; ++i) {
+        const ScreenTable& t = ctx->screen[i];
+        if (t.width == f.width && t.height == f.height &&
+            std::memcmp(&t.tan_half_fov, &f.tan_half_fov, sizeof(float)) == 0) {
+            *out = t.d;
+            return VT_OK;
+        }
+    }
+    if (!create || ctx->n_screen >= kScreenTables) return VT_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        return VT_OK;
+    }
+    if (cs != cudaStreamCaptureStatusNone) return VT_OK;
+    ScreenTable t;
+    t.width = f.width;
+    t.height = f.height;
+    t.tan_half_fov = f.tan_half_fov;
+    const size_t n = (size_t)f.width + (size_t)f.height;
+    VT_CUDA(ctx, cudaMalloc(&t.d, n * sizeof(float4)));
+    k_screen_table<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, st>>>(f, t.d);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaFree(t.d);
+        return check_cuda(ctx, e, "screen table");
+    }
+    ctx->screen[ctx->n_screen++] = t;
+    *out = t.d;
+    return VT_OK;
+}
+
 vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p,
-                               uint4* d_out, cudaStream_t stream, bool stats, int row0, int row1, bool allow_defer) {
+                               uint4* d_out, cudaStream_t stream, bool stats, int row0, int row1, bool allow_defer,
+                               bool new_table) {
     FrameParams f = make_frame(cam, p);
     if (row1 < 0) row1 = cam->height;
     f.row0 = row0;
@@ -372,6 +432,10 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
             k_render_persist<false><<<blocks, kPersistBlock, 0, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
         VT_CUDA(ctx, cudaGetLastError());
         return VT_OK;
+    }
+    {
+        vt_status s = screen_table(ctx, f, stream, new_table, &f.screen);
+        if (s) return s;
     }
     const bool defer = allow_defer && (p->rays & VT_RAYS_BOUNCE) && !stats && !checked;
     if (defer) {

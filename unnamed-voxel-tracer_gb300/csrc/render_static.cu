@@ -61,7 +61,8 @@ extern "C" vt_status vt_render_host_static(vt_ctx* ctx, const vt_world* world, c
     void* d = nullptr;
     s = static_records(ctx, &d);
     if (s) return s;
-    s = vt::launch_render(ctx, world, cam, params, reinterpret_cast<uint4*>(d), ctx->stream, false);
+    s = vt::launch_render(ctx, world, cam, params, reinterpret_cast<uint4*>(d), ctx->stream, false, 0, -1, false,
+                          false);  // no allocation: an existing screen table only
     if (s) return s;
     VT_CUDA(ctx, cudaMemcpyAsync(h_out, d, (size_t)pixels * sizeof(vt_hit), cudaMemcpyDeviceToHost, ctx->stream));
     return vt_sync(ctx, ctx->stream);

@@ -37,6 +37,7 @@ struct FrameParams {
     int row0, row_end;  // rows [row0, row_end) of the image this launch renders
     void* bounce_jobs;       // non-null: bounce rays are queued here (BounceJob), not traced inline
     unsigned* bounce_count;  // the queue's length
+    const float4* screen;    // the frame's screen table (ScreenTable), or null: computed per block
 };
 
 // The per-pixel screen coordinates, each a function of the column or of the
@@ -77,6 +78,19 @@ __device__ __forceinline__ PixelUV pixel_uv(const FrameParams& f, int px, int py
     uv.cv = centre_v(f, py);
     uv.gu = vignette_u(uv.cu);
     uv.gv = vignette_v(uv.cv);
+    return uv;
+}
+
+// PixelUV of pixel (px, py) from the frame's screen table.
+__device__ __forceinline__ PixelUV table_uv(const FrameParams& f, int px, int py) {
+    const float4 c = __ldg(f.screen + px), r = __ldg(f.screen + f.width + py);
+    PixelUV uv;
+    uv.ru = c.x;
+    uv.cu = c.y;
+    uv.gu = c.z;
+    uv.rv = r.x;
+    uv.cv = r.y;
+    uv.gv = r.z;
     return uv;
 }
 

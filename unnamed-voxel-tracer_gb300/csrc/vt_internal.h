@@ -67,6 +67,19 @@ constexpr int kMaxImageSide = 32768;
 
 }  // namespace vt
 
+namespace vt {
+// The screen coordinates of one image size and field of view: a float4 per
+// column {ray u, centre u, vignette column factor, 0} followed by one per row
+// {ray v, centre v, vignette row factor, 0}.  Written once, then only read
+// (frames on other streams may be reading it), freed with the context.
+struct ScreenTable {
+    int width = 0, height = 0;
+    float tan_half_fov = 0.0f;
+    float4* d = nullptr;
+};
+constexpr int kScreenTables = 8;
+}  // namespace vt
+
 struct vt_ctx {
     int device = 0;
     int sm_count = 0;
@@ -99,7 +112,9 @@ struct vt_ctx {
     unsigned* d_bounce_ctr = nullptr;  // {queued, taken}
     size_t bounce_capacity = 0;
     cudaEvent_t ev_bounce = nullptr;   // the last deferred frame is done with the queue
-    void* d_screen = nullptr;          // per-column and per-row composite coordinates (float2 each)
+    // screen tables of the frame sizes rendered so far (see screen_table)
+    vt::ScreenTable screen[vt::kScreenTables];
+    int n_screen = 0;
     int bounce_blocks = 0;
 };
 
@@ -185,8 +200,11 @@ vt_status check_frame_args(vt_ctx* ctx, const vt_world* world, const vt_camera* 
 // allow_defer: bounce rays may go through the context's deferred bounce pass
 // (single-frame entry points; not inside graph capture or allocation-free
 // calls).
+// new_table: the frame's screen table may be made here (an allocation and one
+// synchronisation, once per image size and field of view).
 vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* p, uint4* d_out,
-                        cudaStream_t stream, bool stats, int row0 = 0, int row1 = -1, bool allow_defer = false);
+                        cudaStream_t stream, bool stats, int row0 = 0, int row1 = -1, bool allow_defer = false,
+                        bool new_table = true);
 struct FrameParams;
 // The deferred bounce pass: queue buffers for `pixels` rays, and the trace +
 // shade kernels for a frame whose render kernel queued them.
