@@ -120,3 +120,49 @@ def test_tiny_step_limits_in_a_frame(vt, oracle, ctx, steps):
     p = vt.default_params(rays=3, sun_dir=(0.3, 0.8, 0.5), max_steps=steps, shadow_max_steps=steps)
     gpu, ref = frame_both(vt, oracle, ctx, mats, cam, p)
     compare(gpu, ref)
+
+
+@pytest.mark.parametrize("size", [(32768, 2), (3, 32768)])
+def test_largest_image_sides(vt, oracle, ctx, size):
+    """Frames at the largest accepted width and height (32768)."""
+    mats = terrain(vt, (64, 48, 64), seed=6)
+    cam = look_at(vt, (32, 40, 30), (32, 10, 60), *size, fov=math.radians(20))
+    gpu, ref = frame_both(vt, oracle, ctx, mats, cam, vt.default_params(**PARAMS))
+    compare(gpu, ref)
+    assert (gpu["flags"] & vt.HIT_PRIMARY).mean() > 0.2
+
+
+@pytest.mark.parametrize("dims", [(8192, 8, 4), (4, 8192, 8), (8, 4, 8192)])
+def test_longest_world_axes(vt, oracle, ctx, dims):
+    """Worlds at the largest accepted extent (8192) along one axis: rays along
+    and across the long axis."""
+    rng = np.random.default_rng(dims.index(8192))
+    X, Y, Z = dims
+    mats = (rng.random((Z, Y, X)) < 0.02).astype(np.uint8) * 5
+    w = make_world(vt, ctx, mats)
+    try:
+        o, d = random_rays(rng, dims, 6000)
+        long_axis = dims.index(8192)
+        d[:2000, long_axis] = np.where(d[:2000, long_axis] >= 0, 50.0, -50.0)  # mostly along the long axis
+        d = d.astype(np.float32)
+        for steps in (64, 20000):
+            compare(vt.trace_rays(ctx, w, o, d, steps), oracle.trace_rays(oracle.OracleWorld(mats), o, d, steps),
+                    rgb_tol=0)
+    finally:
+        w.close()
+
+
+def test_sizes_beyond_the_limits_are_rejected(vt, ctx):
+    for dims in ((8193, 4, 4), (0, 4, 4), (4, 4, -1)):
+        with pytest.raises(vt.VTError):
+            vt.World(ctx, dims)
+    mats = np.zeros((8, 8, 8), np.uint8)
+    w = make_world(vt, ctx, mats)
+    try:
+        for size in ((32769, 2), (2, 32769), (0, 5)):
+            cam = look_at(vt, (4, 4, -4), (4, 4, 4), 1, 1)
+            cam.width, cam.height = size
+            with pytest.raises(vt.VTError):
+                vt.render_host(ctx, w, cam, vt.default_params(**PARAMS), np.zeros(max(1, size[0] * size[1]), vt.HIT_DTYPE))
+    finally:
+        w.close()
