@@ -28,7 +28,7 @@ __device__ __forceinline__ bool trace_any(const WorldView& w, const Coarse& coar
 }
 
 // uv: the pixel's screen coordinates (pixel_uv(f, px, py); the frame kernel
-// reads them from per-block tables).
+// reads them from the frame's screen table or its per-block tables).
 template <bool STATS, bool CHECKED, class Coarse>
 __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
                                               const FrameParams& f, int px, int py, const PixelUV& uv,
