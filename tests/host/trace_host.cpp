@@ -90,7 +90,8 @@ static void distances(const int cd[3], const std::vector<unsigned long long>& ma
     bdist.assign(vt::kOctants * nch * 512, 0);
     cdist.assign(vt::kOctants * cstride, 0);
     for (int o = 0; o < vt::kOctants; ++o) {
-        std::vector<unsigned char> bd = cheb(bocc, gx, gy, gz, vt::kFlatY, o), cdd = cheb(cocc, cd[0], cd[1], cd[2], 1, o);
+        std::vector<unsigned char> bd = cheb(bocc, gx, gy, gz, vt::flat_y((unsigned)o), o),
+                                   cdd = cheb(cocc, cd[0], cd[1], cd[2], 1, o);
         for (int z = 0; z < gz; ++z)
             for (int y = 0; y < gy; ++y)
                 for (int x = 0; x < gx; ++x) {

@@ -455,9 +455,9 @@ struct Walker {
         for (int i = 0; i < 3; ++i) {
             const int u = c[i] >> sh;
             // a brick distance d promises d-1 bricks ahead across and
-            // (d-1)/kFlatY vertically (kFlatY-weighted Chebyshev distance)
-            // (rad >= 1 in an empty unit: an unsigned quotient, a shift)
-            const int ri = (i == 1 && sh == 2) ? (int)((unsigned)(rad - 1) / (unsigned)kFlatY) + 1 : rad;
+            // (d-1)/flat_y(oct) vertically (the field's weighted Chebyshev
+            // distance; rad >= 1 in an empty unit, so the quotient is a shift)
+            const int ri = (i == 1 && sh == 2) ? (int)((unsigned)(rad - 1) >> ((oct & 2u) ? 0 : kFlatYShift)) + 1 : rad;
             K[i] = r.pos[i] ? (u + ri) * (1 << sh) : (u - (ri - 1)) * (1 << sh);
             tK[i] = ptime(r, i, K[i]);
         }

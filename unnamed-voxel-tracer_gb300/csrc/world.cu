@@ -123,7 +123,7 @@ __global__ void k_dist_pass(const unsigned long long* __restrict__ mask, const u
     if (axis > 0) in += (size_t)(v & ((1u << axis) - 1u)) * stride;
     out += (size_t)v * stride;
     const int dlo = fwd ? 0 : -kDistCap, dhi = fwd ? kDistCap : 0;
-    const int wgt = level == 0 && axis == 1 ? kFlatY : 1;
+    const int wgt = level == 0 && axis == 1 ? flat_y(v) : 1;  // v's bit 1 is the y direction
     const size_t total = (size_t)ext.x * ext.y * ext.z;
     for (size_t lin = blockIdx.x * (size_t)blockDim.x + threadIdx.x; lin < total; lin += (size_t)gridDim.x * blockDim.x) {
         const int x = lo.x + (int)(lin % ext.x), y = lo.y + (int)((lin / ext.x) % ext.y),
@@ -201,12 +201,12 @@ void brick_passes(vt_world* w, cudaStream_t st, const int3 lo[3], const int3 ext
 
 // After the bricks of box [blo, blo + bext) changed occupancy only these
 // cells can change: the x pass in the box +- (R, 0, 0), the y pass in the box
-// +- (R, RY, 0), the z pass in the box +- (R, RY, R), with R = kDistCap and
-// RY = kDistCap / kFlatY (a y offset beyond RY weighs more than the cap).
-// Recomputing exactly those boxes, in pass order, from the current masks
-// leaves every buffer equal to a full rebuild.
+// +- (R, RY, 0), the z pass in the box +- (R, RY, R), with R = RY = kDistCap
+// (the upward octants' fields weigh y offsets by 1, so their y pass reaches
+// as far as the others).  Recomputing exactly those boxes, in pass order, from
+// the current masks leaves every buffer equal to a full rebuild.
 void edit_boxes(int3 blo, int3 bext, int3 lo[3], int3 ext[3]) {
-    const int R = kDistCap, RY = kDistCap / kFlatY;
+    const int R = kDistCap, RY = kDistCap / flat_y(2u);
     lo[0] = make_int3(blo.x - R, blo.y, blo.z);
     ext[0] = make_int3(bext.x + 2 * R, bext.y, bext.z);
     lo[1] = make_int3(blo.x - R, blo.y - RY, blo.z);
