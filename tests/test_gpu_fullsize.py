@@ -6,7 +6,9 @@
     primary + shadow + bounce rays, every 16th row against the oracle;
   - size-independent properties of the full frames: the records of the
     batched graph and of the pinned-memory path equal vt_render's, and the
-    instrumented kernel's counters equal the oracle's on sampled rows.
+    instrumented kernel's counters equal the oracle's on sampled rows;
+  - the batch workload's scenes up to 300 voxels on a side, as one batch
+    graph, every 4th row of every job against the oracle (about 11 M rays).
 
 The oracle runs multithreaded on the host (about a second per 1080p frame on
 16 cores)."""
@@ -100,3 +102,42 @@ def test_config2_world_4k_with_bounce_rays_sampled_rows(vt, ctx, oracle):
         assert st["bounce_rays"] > 100000 and st["bounce_hits"] > 1000
     finally:
         w.close()
+
+
+def test_config3_batch_against_oracle_sampled_rows(vt, ctx, oracle):
+    """The 64-scene batch workload's first scenes up to 300 voxels on a side
+    (log-uniform cube worlds, 1-8 cameras each at 320x240 to 1920x1080), run
+    as one batch graph: every 4th row of every job against the oracle, over a
+    million rays in all."""
+    import scenes
+    sc, params = scenes.config3()
+    picked = [(d, cams) for d, cams in sc if d.dims[0] <= 300][:8]
+    worlds, jobs, owners = [], [], []
+    try:
+        for d, cams in picked:
+            mats = vt.gen_world(d)
+            w = vt.World(ctx, tuple(d.dims))
+            w.upload_dense(mats)
+            worlds.append(w)
+            ow = oracle.OracleWorld(mats)
+            for cam in cams:
+                jobs.append((w, cam, ctx.alloc(cam.width * cam.height * 16)))
+                owners.append(ow)
+        batch = vt.Batch(ctx, jobs, params)
+        batch.launch()
+        ctx.sync()
+        rays = 0
+        for (w, cam, buf), ow in zip(jobs, owners):
+            got = buf.download(np.zeros(cam.width * cam.height, vt.HIT_DTYPE))
+            ref, st = oracle.render(ow, vt.default_palette(), cam, params, threads=THREADS, row_step=4)
+            rows = np.arange(0, cam.height, 4)
+            compare(got.reshape(cam.height, cam.width)[rows].reshape(-1),
+                    ref.reshape(cam.height, cam.width)[rows].reshape(-1))
+            rays += st["primary_rays"] + st["shadow_rays"]
+        batch.close()
+        assert rays > 1_000_000
+    finally:
+        for _, _, buf in jobs:
+            buf.free()
+        for w in worlds:
+            w.close()
