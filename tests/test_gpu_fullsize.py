@@ -8,7 +8,9 @@
     batched graph and of the pinned-memory path equal vt_render's, and the
     instrumented kernel's counters equal the oracle's on sampled rows;
   - the batch workload's scenes up to 300 voxels on a side, as one batch
-    graph, every 4th row of every job against the oracle (about 11 M rays).
+    graph, every 4th row of every job against the oracle (about 11 M rays);
+  - the shading benchmark at full size (16 views of 512x512): one fused
+    forward + backward over all views against the FP64 gradient.
 
 The oracle runs multithreaded on the host (about a second per 1080p frame on
 16 cores)."""
@@ -141,3 +143,65 @@ def test_config3_batch_against_oracle_sampled_rows(vt, ctx, oracle):
             buf.free()
         for w in worlds:
             w.close()
+
+
+def test_config4_full_shading_step_against_fp64(vt, ctx, oracle):
+    """The shading benchmark at full size: 256^3 world, 16 views of 512x512,
+    targets rendered with the hidden palette and sun; one fused forward +
+    backward over all views (vt_shade_backward_views) against the FP64
+    gradient summed over the views (within 1e-4 of each group's largest
+    component), and the forward image of every view against the FP64 colours."""
+    from concurrent.futures import ThreadPoolExecutor
+    import scenes
+    desc, cams, (pal, alb, sun), (hpal, hsun) = scenes.config4()
+    mats = vt.gen_world(desc)
+    w = vt.World(ctx, tuple(desc.dims))
+    bufs = []
+    try:
+        w.upload_dense(mats)
+        n = cams[0].width * cams[0].height
+        prim = vt.default_params(rays=vt.RAYS_PRIMARY, shade=vt.SHADE_NONE)
+        hits = [ctx.alloc(n * 16) for _ in cams]
+        targets = [ctx.alloc(n * 12) for _ in cams]
+        rgbs = [ctx.alloc(n * 12) for _ in cams]
+        bufs = hits + targets + rgbs
+        for c, hb in zip(cams, hits):
+            vt.render(ctx, w, c, prim, hb)
+        hidden = vt.Shading(ctx, w, hpal, alb, hsun)
+        for c, hb, tb in zip(cams, hits, targets):
+            hidden.forward(c, hb, tb)
+        hidden.close()
+        sh = vt.Shading(ctx, w, pal, alb, sun)
+        sh.zero_grad()
+        sh.backward_views(cams, hits, targets)
+        g = sh.grads()
+        sh.forward_views(cams, hits, rgbs)
+        ctx.sync()
+        sh.close()
+        recs = [hb.download(np.zeros(n, vt.HIT_DTYPE)) for hb in hits]
+        tgts = [tb.download(np.zeros((n, 3), np.float32)) for tb in targets]
+        imgs = [rb.download(np.zeros((n, 3), np.float32)) for rb in rgbs]
+        ow = oracle.OracleWorld(mats)
+
+        def ref(v):
+            return oracle.shade_grad_f64(ow, cams[v], recs[v], pal, alb, sun, 0.2, 0.8, 512, tgts[v])
+
+        loss, rpal, rsun, ralb, lit = 0.0, np.zeros((256, 3)), np.zeros(3), np.zeros(mats.size), 0
+        with ThreadPoolExecutor(max_workers=4) as ex:
+            for img, r in zip(imgs, ex.map(ref, range(len(cams)))):
+                assert np.abs(img - r["rgb"]).max() <= 1e-6
+                loss += r["loss"]
+                rpal += r["palette"]
+                rsun += r["sun"]
+                ralb += r["albedo"]
+                lit += int((r["vis"] != 0).sum())
+        rel = 1e-4
+        assert g["loss"] == pytest.approx(loss, rel=rel)
+        assert np.abs(g["palette"] - rpal).max() <= rel * np.abs(rpal).max()
+        assert np.abs(g["sun"] - rsun).max() <= rel * np.abs(rsun).max()
+        assert np.abs(g["albedo"] - ralb).max() <= rel * np.abs(ralb).max()
+        assert lit > 100000
+    finally:
+        for b in bufs:
+            b.free()
+        w.close()
