@@ -63,7 +63,8 @@ const char* vt_status_string(vt_status s);
 vt_status   vt_ctx_create(int32_t device, vt_ctx** out);
 vt_status   vt_ctx_destroy(vt_ctx* ctx);
 const char* vt_last_error_string(const vt_ctx* ctx);
-/* Waits for `stream`, then reads and clears the context's device status word. */
+/* Waits for `stream`, then reads and clears the context's device status word
+ * (skipped while no checked or instrumented launch can have set it). */
 vt_status   vt_sync(vt_ctx* ctx, vt_stream stream);
 /* Device name and SM count of the context's device. */
 vt_status   vt_device_info(vt_ctx* ctx, char* name, int32_t name_len, int32_t* sm_count);
