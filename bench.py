@@ -290,11 +290,13 @@ def measure_mode_r(vt, ctx, torch, mats, cams, flush) -> dict:
     (traceMap stepping one voxel or sub-voxel per iteration, 192 iterations
     for primary and 48 for shadow rays, map.glsl:83-168, secondary.comp.glsl)."""
     import brickmap
+    sys.path.insert(0, str(ROOT / "tests"))
+    import refworld   # the seeded sub-voxel models of the tests
     rng = np.random.default_rng(SEED)
     chunks, data = brickmap.build_map(mats, np.arange(256, dtype=np.uint32) % 8)
     bm = vt.Brickmap(ctx)
     bm.upload(chunks, data)
-    bm.set_atlas(brickmap.build_atlas(brickmap.random_models(rng, 8)), 8)
+    bm.set_atlas(brickmap.build_atlas(refworld.random_models(rng, 8)), 8)
     out = ctx.alloc(IMAGE[0] * IMAGE[1] * 32)
     sh = torch.cuda.current_stream().cuda_stream
 

@@ -22,7 +22,8 @@
  *     cudaStream_t passed as void*, NULL = the legacy default stream).  Device
  *     pointers named d_* must be device memory of the context's device.
  *   - vt_sync() waits for a stream and surfaces the device status word that the
- *     checked kernels write (VT_ERR_DEVICE_OOB, VT_ERR_TIMEOUT).
+ *     checked kernels write (VT_ERR_DEVICE_OOB); vt_wait() is the same with a
+ *     deadline (VT_ERR_TIMEOUT when the stream is still busy at the deadline).
  *   - One vt_ctx per host thread; the library holds no global mutable state
  *     besides CUDA's own and the fixed device array behind
  *     vt_render_host_static.
@@ -46,7 +47,7 @@ typedef int32_t vt_status;
 #define VT_ERR_OOM         2  /* device or host allocation failed */
 #define VT_ERR_CUDA        3  /* a CUDA runtime call failed (message has the CUDA error) */
 #define VT_ERR_DEVICE_OOB  4  /* a checked kernel saw an out-of-range index */
-#define VT_ERR_TIMEOUT     5  /* a bounded device-side wait gave up */
+#define VT_ERR_TIMEOUT     5  /* a bounded wait (vt_wait) ran out before the stream was done */
 #define VT_ERR_NO_DEVICE   6  /* no CUDA device / driver */
 #define VT_ERR_FORMAT      7  /* malformed input file (.vox) */
 #define VT_ERR_STATE       8  /* call not valid in the object's current state */
@@ -66,6 +67,12 @@ const char* vt_last_error_string(const vt_ctx* ctx);
 /* Waits for `stream`, then reads and clears the context's device status word
  * (skipped while no checked or instrumented launch can have set it). */
 vt_status   vt_sync(vt_ctx* ctx, vt_stream stream);
+/* vt_sync with a deadline, for frame loops with a time budget (the reference
+ * blocks in its GL fence without one, game.zig:249-256): polls `stream` for at
+ * most timeout_us microseconds and returns VT_ERR_TIMEOUT if it is still busy
+ * then.  The queued work is untouched and keeps running; the caller may wait
+ * again.  Once the stream is done it behaves as vt_sync. */
+vt_status   vt_wait(vt_ctx* ctx, vt_stream stream, int64_t timeout_us);
 /* Device name and SM count of the context's device. */
 vt_status   vt_device_info(vt_ctx* ctx, char* name, int32_t name_len, int32_t* sm_count);
 
@@ -80,6 +87,18 @@ vt_status vt_memcpy_d2h(vt_ctx* ctx, void* h_dst, const void* d_src, size_t nbyt
 vt_status vt_memset_d(vt_ctx* ctx, void* d_dst, int32_t value, size_t nbytes, vt_stream stream);
 vt_status vt_stream_create(vt_ctx* ctx, vt_stream* out);
 vt_status vt_stream_destroy(vt_ctx* ctx, vt_stream stream);
+
+/* Testing hooks for the allocation-failure paths (no counterpart in the
+ * reference, whose block allocator panics when it cannot grow,
+ * src/engine/graphics/gpu_block_allocator.zig:22).  Every device and pinned
+ * host allocation the library makes goes through one wrapper:
+ *   vt_debug_fail_alloc(n)   the n-th next allocation (n >= 1) fails as if the
+ *                            device were out of memory, then the hook disarms;
+ *                            n = 0 disarms it.  Process-wide.
+ *   vt_debug_alloc_counts    allocations made so far, and those still live
+ *                            (made minus freed), process-wide. */
+void vt_debug_fail_alloc(int64_t n);
+void vt_debug_alloc_counts(uint64_t* made, int64_t* live);
 
 /* ------------------------------------------------------------------- world
  * Mode-P world: a dense grid of uint8 materials (0 = air), stored on the device
@@ -224,12 +243,16 @@ vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* ca
  * that must not call cudaMalloc once running (it can synchronize the device).
  * vt_render_host stages the records in a buffer the context allocates on
  * first use; this call stages them in a fixed device array compiled into the
- * library (VT_STATIC_MAX_PIXELS records, 4 MiB, held by every GPU that loads
- * the library until exit) and allocates nothing.
+ * library (VT_STATIC_MAX_PIXELS records, 4 MiB per device) and allocates
+ * nothing.  It traces bounce rays inline (no deferred queue) and makes no
+ * screen table (it uses one made earlier for the same image size, else the
+ * kernel's per-block coordinates).
  *   - Frames larger than VT_STATIC_MAX_PIXELS pixels are rejected (VT_ERR_ARG).
- *   - The first call on a device looks the array's device address up
- *     (cudaGetSymbolAddress, with that device current); make that first call
- *     before any stream capture.
+ *   - The array is placed on a device when the first context for that device
+ *     is created: vt_ctx_create looks its device address up
+ *     (cudaGetSymbolAddress, with that device current), which is when CUDA's
+ *     lazy module loading loads it.  It stays until the process exits.  This
+ *     call therefore neither loads a module nor allocates.
  *   - All calls share the one array: calls whose work overlaps on the GPU
  *     (several host threads, several contexts) race on it. */
 #define VT_STATIC_MAX_PIXELS 262144

@@ -74,7 +74,7 @@ def load() -> C.CDLL:
                                       C.POINTER(C.c_float), C.POINTER(VtoRefHit_t)]
         lib.vto_shade_grad_f64.argtypes = [C.POINTER(VtoWorld_t), C.POINTER(vt.Camera_t), P, P, P,
                                            C.POINTER(C.c_double), C.c_double, C.c_double, C.c_int32, P, P, P, P,
-                                           P, P, P, C.POINTER(C.c_double)]
+                                           P, P, P, C.POINTER(C.c_double), P, P, C.POINTER(C.c_double)]
         lib.vto_shade_grad_f64.restype = C.c_int32
         lib.vto_trace_entities.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
                                            C.POINTER(VtoRefHit_t)]
@@ -188,6 +188,9 @@ def shade_grad_f64(world: OracleWorld, cam, hits: np.ndarray, palette, albedo, s
     g_pal = np.zeros(768, np.float64)
     g_alb = np.zeros(X * Y * Z, np.float64) if alb is not None else None
     g_sun = (C.c_double * 3)()
+    a_pal = np.zeros(768, np.float64)
+    a_alb = np.zeros(X * Y * Z, np.float64) if alb is not None else None
+    a_sun = (C.c_double * 3)()
     tgt = None if target is None else np.ascontiguousarray(target, np.float32).reshape(-1)
     vin = None if vis_in is None else np.ascontiguousarray(vis_in, np.uint8).reshape(-1)
     rc = load().vto_shade_grad_f64(
@@ -195,11 +198,13 @@ def shade_grad_f64(world: OracleWorld, cam, hits: np.ndarray, palette, albedo, s
         alb.ctypes.data if alb is not None else None, (C.c_double * 3)(*sun), ambient, diffuse, shadow_max_steps,
         tgt.ctypes.data if tgt is not None else None, vin.ctypes.data if vin is not None else None, vis.ctypes.data,
         rgb.ctypes.data, loss.ctypes.data, g_pal.ctypes.data, g_alb.ctypes.data if g_alb is not None else None,
-        g_sun)
+        g_sun, a_pal.ctypes.data, a_alb.ctypes.data if a_alb is not None else None, a_sun)
     if rc != 0:
         raise ValueError("bad shading arguments")
+    # abs_*: per gradient element, the sum of |per-pixel contribution|
     return {"rgb": rgb.reshape(n, 3), "vis": vis, "loss": float(loss[0]), "palette": g_pal.reshape(256, 3),
-            "albedo": g_alb, "sun": np.array(list(g_sun))}
+            "albedo": g_alb, "sun": np.array(list(g_sun)), "abs_palette": a_pal.reshape(256, 3),
+            "abs_albedo": a_alb, "abs_sun": np.array(list(a_sun))}
 
 
 def render_reference(world: OracleRefWorld, cam) -> np.ndarray:

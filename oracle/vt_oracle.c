@@ -581,7 +581,8 @@ void vto_trace_rays(const vto_world* w, const float* origins, const float* dirs,
 int32_t vto_shade_grad_f64(const vto_world* w, const vt_camera* cam, const vt_hit* hits, const double* pal,
                            const double* alb, const double sun[3], double ka, double kd, int32_t shadow_max_steps,
                            const float* target, const uint8_t* vis_in, uint8_t* vis_out, double* rgb, double* loss,
-                           double* g_pal, double* g_alb, double g_sun[3]) {
+                           double* g_pal, double* g_alb, double g_sun[3], double* a_pal, double* a_alb,
+                           double a_sun[3]) {
     const double len = sqrt(sun[0] * sun[0] + sun[1] * sun[1] + sun[2] * sun[2]);
     if (!(len > 0.0)) return 1;
     const double sn[3] = {sun[0] / len, sun[1] / len, sun[2] / len};
@@ -632,14 +633,22 @@ int32_t vto_shade_grad_f64(const vto_world* w, const vt_camera* cam, const vt_hi
                 if (loss) *loss += diff * diff;
             }
             if (!hit) continue;
+            double aa = 0.0;
             for (int k = 0; k < 3; ++k) {
                 if (g_pal) g_pal[3 * m + k] += g[k] * albv * shade;
+                if (a_pal) a_pal[3 * m + k] += fabs(g[k] * albv * shade);
                 ga += g[k] * pal[3 * m + k] * shade;
+                aa += fabs(g[k] * pal[3 * m + k] * shade);
                 gb += g[k] * pal[3 * m + k] * albv;
             }
             if (g_alb) g_alb[h->voxel] += ga;
-            if (g_sun && lit && ndl > 0.0)
-                for (int k = 0; k < 3; ++k) g_sun[k] += gb * kd * (nrm[k] - ndl * sn[k]) / len;
+            if (a_alb) a_alb[h->voxel] += aa;
+            if (lit && ndl > 0.0)
+                for (int k = 0; k < 3; ++k) {
+                    const double term = gb * kd * (nrm[k] - ndl * sn[k]) / len;
+                    if (g_sun) g_sun[k] += term;
+                    if (a_sun) a_sun[k] += fabs(term);
+                }
         }
     return 0;
 }

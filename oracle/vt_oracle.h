@@ -90,11 +90,16 @@ void vto_trace_rays(const vto_world* w, const float* origins, const float* dirs,
  *     c = pal[m] * alb[v] * (ka + kd * max(0, n . s/|s|) * V),  L = sum (c - target)^2
  * V is read from vis_in (1 = lit) when not NULL, else traced from the hit with
  * the mode-P traversal (shadow origin as in the render path); vis_out, rgb,
- * g_pal (768), g_alb (X*Y*Z) may be NULL.  Gradients are added to the outputs. */
+ * g_pal (768), g_alb (X*Y*Z) may be NULL.  Gradients are added to the outputs.
+ * a_pal, a_alb, a_sun (each NULL or shaped like its gradient) receive the sum
+ * of the absolute values of the per-pixel contributions to each gradient
+ * element: the scale of a float32 accumulation's rounding error in that
+ * element, which a parity check uses as its absolute floor. */
 int32_t vto_shade_grad_f64(const vto_world* w, const vt_camera* cam, const vt_hit* hits, const double* pal,
                            const double* alb, const double sun[3], double ka, double kd, int32_t shadow_max_steps,
                            const float* target, const uint8_t* vis_in, uint8_t* vis_out, double* rgb, double* loss,
-                           double* g_pal, double* g_alb, double g_sun[3]);
+                           double* g_pal, double* g_alb, double g_sun[3], double* a_pal, double* a_alb,
+                           double a_sun[3]);
 
 /* The deterministic sine/cosine used for bounce directions. */
 float vto_sinf(float x);

@@ -1,6 +1,7 @@
 """Worlds in the reference's own format, for the mode-R oracle checks (the
 builders live in the package, unnamed-voxel-tracer_gb300/brickmap.py; the
-.vox writer/reader and the ray sampler are test helpers).
+random models, the .vox writer/reader and the ray sampler are test and
+benchmark helpers).
 
 The reference stores a 512^3 voxel map as a 64^3 table of brick indices
 (0 = empty, else brick + 1; index x + 64*(y + 64*z), voxel.zig:21-23) and a
@@ -14,7 +15,57 @@ from __future__ import annotations
 import numpy as np
 
 
-from brickmap import build_atlas, build_map, random_models  # noqa: E402,F401  (the package's builders)
+from brickmap import build_atlas, build_map  # noqa: E402,F401  (the package's builders)
+
+
+def random_models(rng: np.random.Generator, n: int, full: bool = False) -> list[np.ndarray]:
+    """n models, each an (8, 8, 8) [z, y, x] array of RGBA8 texels (0 = empty)."""
+    out = []
+    for i in range(n):
+        density = 1.0 if full else rng.uniform(0.2, 1.0)
+        keep = rng.random((8, 8, 8)) < density
+        rgb = rng.integers(1, 256, size=(8, 8, 8, 3), dtype=np.uint32)
+        tex = rgb[..., 0] | (rgb[..., 1] << 8) | (rgb[..., 2] << 16) | (np.uint32(255) << 24)
+        out.append(np.where(keep, tex, 0).astype(np.uint32))
+    return out
+
+
+def tracemap_f64(occupied, o, d, max_steps: int, snap: float):
+    """The reference's traceMap stepping (map.glsl:83-168) restated in float64
+    for worlds whose occupied voxels hold full 8^3 models, so that a voxel's
+    first sub-voxel already hits.  occupied(x, y, z) -> bool; o, d: the ray as
+    traceMap receives it (world units).  snap is the factor of map.glsl:162
+    (0.999 in the reference; a value just below 1 makes the snap vanish).
+    Returns ((x, y, z), face) of the hit voxel, face = 2 axis + (d_axis > 0 ?
+    0 : 1) from the last step's axis (map.glsl:117-125), or None on a miss."""
+    d = [x if x != 0 else 0.001 for x in d]                       # :85-90
+    bound = 8 * 512
+    sgn = [1 if x > 0 else -1 for x in d]
+    pos = [(1 + s) >> 1 for s in sgn]
+    inv = [1.0 / x for x in d]
+    axis = 0
+    g = [int(o[k] * 8.0) for k in range(3)]                        # :100 (truncation)
+    w = [o[k] * 8.0 - g[k] for k in range(3)]
+    step = 0
+    for _ in range(max_steps):
+        if any(v >= bound or v < 0 for v in g):
+            break
+        vox = tuple((g[k] + int(w[k])) >> 3 for k in range(3))    # :108, :114
+        if occupied(*vox):
+            return vox, 2 * axis + (0 if pos[axis] else 1)
+        if step != 3:                                               # :138-144
+            for k in range(3):
+                w[k] += g[k] & 7
+                g[k] -= g[k] & 7
+            step = 3
+        t = [((pos[k] << step) - w[k]) * inv[k] for k in range(3)]  # :157
+        axis = (0 if t[0] < t[2] else 2) if t[0] < t[1] else (1 if t[1] < t[2] else 2)
+        g[axis] += sgn[axis] << step                                # :160
+        tm = t[axis]
+        for k in range(3):
+            w[k] += d[k] * tm                                       # :161
+        w[axis] = ((1 - pos[axis]) << step) * snap                  # :162
+    return None
 
 
 def random_rays(rng: np.random.Generator, lo, hi, n: int):

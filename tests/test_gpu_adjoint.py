@@ -2,14 +2,32 @@
 the FP64 CPU gradient over the same hit and shadow sets, and against central
 finite differences of the GPU forward image (h = 1e-3, shadow set held fixed).
 
-Tolerance: gradients within 1e-4 of the FP64 reference, relative to the
-largest component of each parameter group; forward colours within 1e-6."""
+Tolerance, element by element (grad_close): |g - g64| <= REL |g64| + FLOOR a,
+where a is the element's sum of |per-pixel contributions| (from the FP64
+oracle).  REL = 1e-4 is the bar itself; FLOOR = 1e-5 (about 170 float32 ulps
+of a) only matters where contributions cancel, since a float32 sum of many
+terms is accurate relative to the sum of their magnitudes, not to their
+(possibly near-zero) total.  Forward colours within 1e-6."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 REL = 1e-4
+FLOOR = 1e-5
+
+
+def grad_close(got, ref, abs_sum, what):
+    """Every element of a gradient group within REL of the FP64 value, with
+    the absolute floor FLOOR * (its sum of |contributions|)."""
+    got, ref, a = (np.asarray(x, np.float64).reshape(-1) for x in (got, ref, abs_sum))
+    err = np.abs(got - ref)
+    tol = REL * np.abs(ref) + FLOOR * a
+    bad = np.flatnonzero(err > tol)
+    assert bad.size == 0, (f"{what}: {bad.size} of {ref.size} elements off, worst {bad[np.argmax(err[bad] / tol[bad])]}"
+                           f": got {got[bad[0]]!r} want {ref[bad[0]]!r} (sum |terms| {a[bad[0]]!r})")
+    # the number of elements held to the relative bar alone (err <= REL |g64|)
+    return int((err <= REL * np.abs(ref)).sum())
 
 
 @pytest.fixture(scope="module")
@@ -69,6 +87,7 @@ def test_backward_matches_fp64_gradient(vt, ctx, oracle, scene):
     sh = s["sh"]
     sh.zero_grad()
     ref_loss, ref_pal, ref_alb, ref_sun = 0.0, np.zeros((256, 3)), np.zeros(s["mats"].size), np.zeros(3)
+    abs_pal, abs_alb, abs_sun = np.zeros((256, 3)), np.zeros(s["mats"].size), np.zeros(3)
     for cam, hb, tgt in zip(s["cams"], s["hits"], s["targets"]):
         dt = ctx.alloc(tgt.nbytes)
         dt.upload(tgt)
@@ -81,11 +100,14 @@ def test_backward_matches_fp64_gradient(vt, ctx, oracle, scene):
         ref_pal += r["palette"]
         ref_alb += r["albedo"]
         ref_sun += r["sun"]
+        abs_pal += r["abs_palette"]
+        abs_alb += r["abs_albedo"]
+        abs_sun += r["abs_sun"]
     g = sh.grads()
     assert g["loss"] == pytest.approx(ref_loss, rel=REL)
-    assert np.abs(g["palette"] - ref_pal).max() <= REL * np.abs(ref_pal).max()
-    assert np.abs(g["albedo"] - ref_alb).max() <= REL * np.abs(ref_alb).max()
-    assert np.abs(g["sun"] - ref_sun).max() <= REL * np.abs(ref_sun).max()
+    grad_close(g["palette"], ref_pal, abs_pal, "palette")
+    assert grad_close(g["albedo"], ref_alb, abs_alb, "albedo") > 1000
+    grad_close(g["sun"], ref_sun, abs_sun, "sun")
     assert (np.abs(ref_pal).sum(1) > 0).sum() >= 20 and np.count_nonzero(ref_alb) > 1000
 
 

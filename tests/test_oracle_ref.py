@@ -8,9 +8,9 @@ reference sources are present, and their outputs are committed as fixtures
   - mode R: vto_tracemap / vto_primary_r restate traceMap and the primary ray
     (map.glsl:83-168, primary.comp.glsl:31-43) and must match bit for bit;
   - mode P: on worlds of full 8^3 models the reference's traceMap is a voxel
-    DDA too; the mode-P traversal must find the same voxel and face for all
-    but a small share of rays (the reference's fractional stepping drifts and
-    snaps to 0.999, map.glsl:157-162, the plane-indexed walk does not);
+    DDA too; on the same rays the mode-P traversal finds the same voxel and
+    face except on a pinned number of pixels, each of them a case of the
+    reference's 0.999 snap (map.glsl:162) or its iteration cap;
   - the sky: SkyDome2 with pow() vs the products used here.
 """
 import ctypes as C
@@ -91,8 +91,22 @@ def test_tracemap_matches_compiled_reference_live(oracle, ref):
             assert list(h.hit_pos) == list(hp) and list(h.normal) == list(nm)
 
 
-def test_mode_p_agrees_with_reference_on_full_models(oracle, ref, vtlib):
-    """With every model a full 8^3 block, both traversals are voxel DDAs."""
+# (camera seed, width, height) -> disagreeing pixels, measured; every one is a snap case
+AGREEMENT_PINS = {(1, 96, 64): 6, (2, 160, 100): 119}
+
+
+@pytest.mark.parametrize("cam_seed,width,height", sorted(AGREEMENT_PINS))
+def test_mode_p_agrees_with_reference_on_full_models(oracle, ref, vtlib, cam_seed, width, height):
+    """With every model a full 8^3 block, both traversals are voxel DDAs.  The
+    same ray (the reference's: origin o + d max(tNear, 0) - 0.001,
+    primary.comp.glsl:41-43) goes through the reference's traceMap (compiled)
+    and the mode-P walk.  They disagree on the pinned number of pixels, and
+    each disagreement is the reference's 0.999 snap (map.glsl:162), shown by
+    the reference's stepping restated in float64 (refworld.tracemap_f64): with
+    the snap it reproduces the compiled reference's voxel and face, with a
+    vanishing snap it reproduces mode P's.  A miss of the reference that mode P
+    hits is its 192-iteration cap (primary.comp.glsl:43) when the float64
+    restatement also misses under the cap and finds mode P's hit without it."""
     desc = vtlib.gen_desc((128, 96, 128), seed=8, trees=25)
     mats = vtlib.gen_world(desc)
     rng = np.random.default_rng(8)
@@ -101,24 +115,42 @@ def test_mode_p_agrees_with_reference_on_full_models(oracle, ref, vtlib):
     rw = oracle.OracleRefWorld(chunks, data, refworld.build_atlas(models))
     ref.ref_set_world(rw.chunks.ctypes.data, rw.data.ctypes.data, rw.atlas.ctypes.data)
     ow = oracle.OracleWorld(mats)
-    cam = vtlib.gen_camera(desc, 1, 96, 64)
+    Z, Y, X = mats.shape
+
+    def occupied(x, y, z):
+        return 0 <= x < X and 0 <= y < Y and 0 <= z < Z and mats[z, y, x] != 0
+
+    cam = vtlib.gen_camera(desc, cam_seed, width, height)
+    assert all(0 < cam.pos[k] < mats.shape[2 - k] for k in range(3))   # inside the grid: tNear < 0
+    o = [float(np.float32(cam.pos[k]) - np.float32(0.001)) for k in range(3)]
     face_of = {(-1, 0, 0): 0, (1, 0, 0): 1, (0, -1, 0): 2, (0, 1, 0): 3, (0, 0, -1): 4, (0, 0, 1): 5}
-    agree = total = 0
+    snapped = capped = checked = 0
+    disagree = []
     for py in range(cam.height):
         for px in range(cam.width):
             d3, v, hp, nm = (C.c_float * 3)(), C.c_uint32(), (C.c_float * 3)(), (C.c_float * 3)()
             ref.ref_primary((C.c_float * 4)(*cam.pos), (C.c_float * 16)(*cam.view), cam.fov, px, py, cam.width,
                             cam.height, d3, C.byref(v), hp, nm)
-            # the same ray through the mode-P traversal, from the camera
-            tr = oracle.trace_one(ow, list(cam.pos)[:3], list(d3), 4096)
-            total += 1
-            if v.value == 0:
-                agree += tr.hit == 0 or tr.t > 190  # the reference stops after 192 iterations
+            d = list(d3)
+            tr = oracle.trace_one(ow, o, d, 4096)
+            want = None if v.value == 0 else (tuple(int(np.floor(hp[k] / 8.0)) for k in range(3)),
+                                               face_of[tuple(int(nm[k]) for k in range(3))])
+            got = (tuple(tr.cell), tr.face) if tr.hit else None
+            if (px * 7 + py * 13) % 97 == 0:   # the float64 restatement against the compiled reference
+                assert refworld.tracemap_f64(occupied, o, d, 192, 0.999) == want, (px, py)
+                checked += 1
+            if got == want:
                 continue
-            cell = tuple(int(np.floor(hp[k] / 8.0)) for k in range(3))
-            face = face_of[tuple(int(nm[k]) for k in range(3))]
-            agree += tr.hit == 1 and tuple(tr.cell) == cell and tr.face == face
-    assert agree / total >= 0.985, agree / total
+            disagree.append((px, py))
+            assert refworld.tracemap_f64(occupied, o, d, 192, 0.999) == want, (px, py)
+            if want is None and refworld.tracemap_f64(occupied, o, d, 4096, 0.999) == got:
+                capped += 1
+                continue
+            assert refworld.tracemap_f64(occupied, o, d, 4096, 1.0 - 1e-9) == got, (px, py, got, want)
+            snapped += 1
+    assert len(disagree) == AGREEMENT_PINS[(cam_seed, width, height)], len(disagree)
+    assert snapped + capped == len(disagree) and checked > 50
+    assert 1.0 - len(disagree) / (cam.width * cam.height) >= 0.99
 
 
 def test_sky_products_match_reference_pow(oracle, ref):

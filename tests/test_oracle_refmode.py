@@ -2,6 +2,7 @@
 reference's own code compiled as C++, and the .vox reader against the
 reference's asset files (where present) and a written-out synthetic file."""
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
@@ -9,7 +10,8 @@ import pytest
 
 import refworld
 
-ASSETS = Path("/root/reference/assets")
+# the reference checkout, where oracle/build_ref.py reads it too
+ASSETS = Path(os.environ.get("REFERENCE_ROOT", "/root/reference")) / "assets"
 # VoxelModelAtlas load order of the reference (game.zig:101-113)
 LOAD_ORDER = ["models", "grass", "grass2", "grass3", "grass4", "grass5", "rock", "flower", "water", "tree",
               "leaves", "dirt", "sand"]

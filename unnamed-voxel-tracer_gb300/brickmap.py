@@ -13,18 +13,6 @@ from __future__ import annotations
 import numpy as np
 
 
-def random_models(rng: np.random.Generator, n: int, full: bool = False) -> list[np.ndarray]:
-    """n models, each an (8, 8, 8) [z, y, x] array of RGBA8 texels (0 = empty)."""
-    out = []
-    for i in range(n):
-        density = 1.0 if full else rng.uniform(0.2, 1.0)
-        keep = rng.random((8, 8, 8)) < density
-        rgb = rng.integers(1, 256, size=(8, 8, 8, 3), dtype=np.uint32)
-        tex = rgb[..., 0] | (rgb[..., 1] << 8) | (rgb[..., 2] << 16) | (np.uint32(255) << 24)
-        out.append(np.where(keep, tex, 0).astype(np.uint32))
-    return out
-
-
 def build_atlas(models: list[np.ndarray]) -> np.ndarray:
     atlas = np.zeros((256, 256, 256), dtype=np.uint32)  # [z, y, x]
     for s, m in enumerate(models):

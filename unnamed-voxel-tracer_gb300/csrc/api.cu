@@ -1,7 +1,10 @@
 // api.cu -- context, status and device-memory entry points of the C ABI.
+#include <atomic>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 
 #include "vt_internal.h"
 
@@ -26,14 +29,76 @@ vt_status check_cuda(vt_ctx* ctx, cudaError_t err, const char* what) {
     return fail(ctx, s, what, err);
 }
 
+namespace {
+// The allocation hook: fail_countdown > 0 makes the allocation that brings it
+// to 0 fail.  made / live count the library's allocations.
+std::atomic<long long> g_fail_countdown{0};
+std::atomic<unsigned long long> g_made{0};
+std::atomic<long long> g_live{0};
+
+bool hook_fails() {
+    long long n = g_fail_countdown.load();
+    while (n > 0) {
+        if (g_fail_countdown.compare_exchange_weak(n, n - 1)) return n == 1;
+    }
+    return false;
+}
+}  // namespace
+
+cudaError_t dev_alloc_raw(void** p, size_t bytes) {
+    *p = nullptr;
+    if (hook_fails()) return cudaErrorMemoryAllocation;
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) {
+        g_made++;
+        g_live++;
+    }
+    return e;
+}
+
+cudaError_t host_alloc_raw(void** p, size_t bytes) {
+    *p = nullptr;
+    if (hook_fails()) return cudaErrorMemoryAllocation;
+    const cudaError_t e = cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+    if (e == cudaSuccess) {
+        g_made++;
+        g_live++;
+    }
+    return e;
+}
+
+cudaError_t dev_free(void* p) {
+    if (!p) return cudaSuccess;
+    const cudaError_t e = cudaFree(p);
+    if (e == cudaSuccess) g_live--;
+    return e;
+}
+
+cudaError_t host_free(void* p) {
+    if (!p) return cudaSuccess;
+    const cudaError_t e = cudaFreeHost(p);
+    if (e == cudaSuccess) g_live--;
+    return e;
+}
+
 vt_status take_status(vt_ctx* ctx, unsigned st) {
     if (!st) return VT_OK;
     VT_CUDA(ctx, cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
-    if (st & kStatusOob) return fail(ctx, VT_ERR_DEVICE_OOB, "a checked kernel saw an out-of-range index");
-    return fail(ctx, VT_ERR_TIMEOUT, "a bounded device wait gave up");
+    return fail(ctx, VT_ERR_DEVICE_OOB, "a checked kernel saw an out-of-range index");
 }
 
 vt_status note_status_writer(vt_ctx* ctx, cudaStream_t st) {
+    // Inside a stream capture nothing runs yet; the graph's launch notes it.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    VT_CUDA(ctx, cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return VT_OK;
+    // ev_status must complete only after every launch that may have set the
+    // word since it was last read: while an earlier writer may be pending (on
+    // any stream), this stream first waits for the event that covers it, so
+    // the new record covers both.  (Without the wait, a vt_sync on a stream
+    // whose writer ended early could declare the word clean while a longer
+    // writer on another stream is still to set it.)
+    if (ctx->status_dirty) VT_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_status, 0));
     ctx->status_dirty = true;
     VT_CUDA(ctx, cudaEventRecord(ctx->ev_status, st));
     return VT_OK;
@@ -43,11 +108,11 @@ vt_status ctx_scratch(vt_ctx* ctx, size_t bytes, void** out) {
     if (bytes > ctx->scratch_bytes) {
         if (ctx->d_scratch) {
             VT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-            cudaFree(ctx->d_scratch);
+            dev_free(ctx->d_scratch);
             ctx->d_scratch = nullptr;
             ctx->scratch_bytes = 0;
         }
-        VT_CUDA(ctx, cudaMalloc(&ctx->d_scratch, bytes));
+        VT_CUDA(ctx, dev_alloc(&ctx->d_scratch, bytes));
         ctx->scratch_bytes = bytes;
     }
     *out = ctx->d_scratch;
@@ -69,7 +134,7 @@ const char* vt_status_string(vt_status s) {
         case VT_ERR_OOM: return "out of memory";
         case VT_ERR_CUDA: return "CUDA error";
         case VT_ERR_DEVICE_OOB: return "device index out of range";
-        case VT_ERR_TIMEOUT: return "device wait timed out";
+        case VT_ERR_TIMEOUT: return "wait timed out";
         case VT_ERR_NO_DEVICE: return "no CUDA device";
         case VT_ERR_FORMAT: return "malformed input";
         case VT_ERR_STATE: return "invalid state";
@@ -94,15 +159,18 @@ vt_status vt_ctx_create(int32_t device, vt_ctx** out) {
         if ((e = cudaGetDeviceProperties(&prop, device)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaGetDeviceProperties"); break; }
         std::snprintf(ctx->name, sizeof(ctx->name), "%s", prop.name);
         ctx->sm_count = prop.multiProcessorCount;
-        if ((e = cudaMalloc(&ctx->d_status, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
+        if ((e = dev_alloc(&ctx->d_status, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
         if ((e = cudaMemset(ctx->d_status, 0, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMemset"); break; }
-        if ((e = cudaMalloc(&ctx->d_counters, kNumCounters * sizeof(unsigned long long))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
-        if ((e = cudaMalloc(&ctx->d_work, kWorkSlots * sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
-        if ((e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_status), sizeof(unsigned), cudaHostAllocDefault)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaHostAlloc"); break; }
+        if ((e = dev_alloc(&ctx->d_counters, kNumCounters * sizeof(unsigned long long))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
+        if ((e = dev_alloc(&ctx->d_work, kWorkSlots * sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaMalloc"); break; }
+        if ((e = host_alloc(&ctx->h_status, sizeof(unsigned))) != cudaSuccess) { s = check_cuda(ctx, e, "cudaHostAlloc"); break; }
         *ctx->h_status = 0;
         if ((e = cudaEventCreateWithFlags(&ctx->ev_status, cudaEventDisableTiming)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaEventCreate"); break; }
         // blocking stream: *_host calls order after work queued on the legacy default stream
         if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamDefault)) != cudaSuccess) { s = check_cuda(ctx, e, "cudaStreamCreate"); break; }
+        // the device address of vt_render_host_static's fixed array, looked up
+        // here so that the entry point itself never loads a module
+        if ((s = static_staging_init(ctx)) != VT_OK) break;
     } while (0);
     if (s != VT_OK) {
         vt_ctx_destroy(ctx);
@@ -124,19 +192,19 @@ vt_status vt_ctx_destroy(vt_ctx* ctx) {
         }
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
-    if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    if (ctx->h_status) host_free(ctx->h_status);
     if (ctx->ev_status) cudaEventDestroy(ctx->ev_status);
-    if (ctx->d_bounce_jobs) cudaFree(ctx->d_bounce_jobs);
-    if (ctx->d_bounce_open) cudaFree(ctx->d_bounce_open);
-    if (ctx->d_bounce_ctr) cudaFree(ctx->d_bounce_ctr);
+    dev_free(ctx->d_bounce_jobs);
+    dev_free(ctx->d_bounce_open);
+    dev_free(ctx->d_bounce_ctr);
     if (ctx->ev_bounce) cudaEventDestroy(ctx->ev_bounce);
-    for (int i = 0; i < ctx->n_screen; ++i) cudaFree(ctx->screen[i].d);
+    for (int i = 0; i < ctx->n_screen; ++i) dev_free(ctx->screen[i].d);
     for (int i = 0; i < kMaxBands; ++i)
         if (ctx->ev_band[i]) cudaEventDestroy(ctx->ev_band[i]);
-    if (ctx->d_scratch) cudaFree(ctx->d_scratch);
-    if (ctx->d_status) cudaFree(ctx->d_status);
-    if (ctx->d_counters) cudaFree(ctx->d_counters);
-    if (ctx->d_work) cudaFree(ctx->d_work);
+    dev_free(ctx->d_scratch);
+    dev_free(ctx->d_status);
+    dev_free(ctx->d_counters);
+    dev_free(ctx->d_work);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return VT_OK;
@@ -168,6 +236,22 @@ vt_status vt_sync(vt_ctx* ctx, vt_stream stream) {
     return take_status(ctx, *ctx->h_status);
 }
 
+vt_status vt_wait(vt_ctx* ctx, vt_stream stream, int64_t timeout_us) {
+    if (!ctx || timeout_us < 0) return VT_ERR_ARG;
+    const cudaStream_t st = (cudaStream_t)stream;
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::microseconds(timeout_us);
+    for (;;) {
+        const cudaError_t q = cudaStreamQuery(st);
+        if (q == cudaSuccess) return vt_sync(ctx, stream);
+        if (q != cudaErrorNotReady) return check_cuda(ctx, q, "cudaStreamQuery");
+        cudaGetLastError();  // a pending stream is no error
+        if (std::chrono::steady_clock::now() >= deadline)
+            return fail(ctx, VT_ERR_TIMEOUT,
+                        "stream still busy after " + std::to_string((long long)timeout_us) + " us");
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
 vt_status vt_device_info(vt_ctx* ctx, char* name, int32_t name_len, int32_t* sm_count) {
     if (!ctx) return VT_ERR_ARG;
     if (name && name_len > 0) std::snprintf(name, (size_t)name_len, "%s", ctx->name);
@@ -178,26 +262,26 @@ vt_status vt_device_info(vt_ctx* ctx, char* name, int32_t name_len, int32_t* sm_
 vt_status vt_device_alloc(vt_ctx* ctx, size_t nbytes, void** d_ptr) {
     if (!ctx || !d_ptr) return VT_ERR_ARG;
     *d_ptr = nullptr;
-    VT_CUDA(ctx, cudaMalloc(d_ptr, nbytes ? nbytes : 1));
+    VT_CUDA(ctx, dev_alloc(d_ptr, nbytes ? nbytes : 1));
     return VT_OK;
 }
 
 vt_status vt_device_free(vt_ctx* ctx, void* d_ptr) {
     if (!ctx) return VT_ERR_ARG;
-    VT_CUDA(ctx, cudaFree(d_ptr));
+    VT_CUDA(ctx, dev_free(d_ptr));
     return VT_OK;
 }
 
 vt_status vt_host_alloc_pinned(vt_ctx* ctx, size_t nbytes, void** h_ptr) {
     if (!ctx || !h_ptr) return VT_ERR_ARG;
     *h_ptr = nullptr;
-    VT_CUDA(ctx, cudaMallocHost(h_ptr, nbytes ? nbytes : 1));
+    VT_CUDA(ctx, host_alloc(h_ptr, nbytes ? nbytes : 1));
     return VT_OK;
 }
 
 vt_status vt_host_free_pinned(vt_ctx* ctx, void* h_ptr) {
     if (!ctx) return VT_ERR_ARG;
-    VT_CUDA(ctx, cudaFreeHost(h_ptr));
+    VT_CUDA(ctx, host_free(h_ptr));
     return VT_OK;
 }
 
@@ -231,6 +315,13 @@ vt_status vt_stream_destroy(vt_ctx* ctx, vt_stream stream) {
     if (!ctx) return VT_ERR_ARG;
     VT_CUDA(ctx, cudaStreamDestroy((cudaStream_t)stream));
     return VT_OK;
+}
+
+void vt_debug_fail_alloc(int64_t n) { g_fail_countdown.store(n > 0 ? (long long)n : 0); }
+
+void vt_debug_alloc_counts(uint64_t* made, int64_t* live) {
+    if (made) *made = g_made.load();
+    if (live) *live = g_live.load();
 }
 
 }  // extern "C"

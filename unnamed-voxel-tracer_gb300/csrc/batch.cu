@@ -125,8 +125,8 @@ vt_status vt_batch_create(vt_ctx* ctx, const vt_job* jobs, int32_t n, const vt_p
         return fail(ctx, VT_ERR_ARG, "batch too large (units >= 2^32)");
     }
     cudaError_t e;
-    if ((e = cudaMalloc(&b->d_jobs, host.size() * sizeof(JobDesc))) != cudaSuccess ||
-        (e = cudaMalloc(&b->d_counter, sizeof(unsigned))) != cudaSuccess ||
+    if ((e = vt::dev_alloc(&b->d_jobs, host.size() * sizeof(JobDesc))) != cudaSuccess ||
+        (e = vt::dev_alloc(&b->d_counter, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMemcpy(b->d_jobs, host.data(), host.size() * sizeof(JobDesc), cudaMemcpyHostToDevice)) != cudaSuccess) {
         vt_batch_destroy(b);
         return check_cuda(ctx, e, "batch upload");
@@ -200,6 +200,8 @@ vt_status vt_batch_launch(vt_batch* b, vt_stream stream) {
         VT_CUDA(ctx, cudaGraphInstantiate(&b->exec, b->graph, 0));
     }
     VT_CUDA(ctx, cudaGraphLaunch(b->exec, st));
+    // checked jobs may set the status word (their capture noted nothing)
+    if (b->params.flags & VT_FLAG_CHECKED) return note_status_writer(ctx, st);
     return VT_OK;
 }
 
@@ -208,8 +210,8 @@ vt_status vt_batch_destroy(vt_batch* b) {
     cudaDeviceSynchronize();
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->d_jobs) cudaFree(b->d_jobs);
-    if (b->d_counter) cudaFree(b->d_counter);
+    if (b->d_jobs) vt::dev_free(b->d_jobs);
+    if (b->d_counter) vt::dev_free(b->d_counter);
     delete b;
     return VT_OK;
 }

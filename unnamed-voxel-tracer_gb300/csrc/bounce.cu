@@ -90,14 +90,14 @@ __global__ void __launch_bounds__(kBounceBlock) k_bounce_finish(WorldView w, Fra
 vt_status bounce_buffers(vt_ctx* ctx, size_t pixels) {
     if (pixels <= ctx->bounce_capacity) return VT_OK;
     VT_CUDA(ctx, cudaDeviceSynchronize());
-    if (ctx->d_bounce_jobs) cudaFree(ctx->d_bounce_jobs);
-    if (ctx->d_bounce_open) cudaFree(ctx->d_bounce_open);
+    if (ctx->d_bounce_jobs) vt::dev_free(ctx->d_bounce_jobs);
+    if (ctx->d_bounce_open) vt::dev_free(ctx->d_bounce_open);
     ctx->d_bounce_jobs = nullptr;
     ctx->d_bounce_open = nullptr;
     ctx->bounce_capacity = 0;
-    VT_CUDA(ctx, cudaMalloc(&ctx->d_bounce_jobs, pixels * sizeof(BounceJob)));
-    VT_CUDA(ctx, cudaMalloc(&ctx->d_bounce_open, pixels));
-    if (!ctx->d_bounce_ctr) VT_CUDA(ctx, cudaMalloc(&ctx->d_bounce_ctr, 2 * sizeof(unsigned)));
+    VT_CUDA(ctx, vt::dev_alloc(&ctx->d_bounce_jobs, pixels * sizeof(BounceJob)));
+    VT_CUDA(ctx, vt::dev_alloc(&ctx->d_bounce_open, pixels));
+    if (!ctx->d_bounce_ctr) VT_CUDA(ctx, vt::dev_alloc(&ctx->d_bounce_ctr, 2 * sizeof(unsigned)));
     if (!ctx->ev_bounce) VT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_bounce, cudaEventDisableTiming));
     ctx->bounce_capacity = pixels;
     return VT_OK;

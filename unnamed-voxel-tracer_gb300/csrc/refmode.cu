@@ -403,9 +403,9 @@ RefView view_of(const vt_brickmap* bm) {
 }
 
 void free_brickmap(vt_brickmap* bm) {
-    if (bm->d_chunks) cudaFree(bm->d_chunks);
-    if (bm->d_data) cudaFree(bm->d_data);
-    if (bm->d_atlas) cudaFree(bm->d_atlas);
+    if (bm->d_chunks) vt::dev_free(bm->d_chunks);
+    if (bm->d_data) vt::dev_free(bm->d_data);
+    if (bm->d_atlas) vt::dev_free(bm->d_atlas);
     delete bm;
 }
 
@@ -425,8 +425,8 @@ vt_status vt_brickmap_create(vt_ctx* ctx, vt_brickmap** out) {
     if (!bm) return fail(ctx, VT_ERR_OOM, "host allocation failed");
     bm->ctx = ctx;
     cudaError_t e;
-    if ((e = cudaMalloc(&bm->d_chunks, 64 * 64 * 64 * sizeof(unsigned))) != cudaSuccess ||
-        (e = cudaMalloc(&bm->d_atlas, (size_t)kModels * 512 * sizeof(unsigned))) != cudaSuccess ||
+    if ((e = vt::dev_alloc(&bm->d_chunks, 64 * 64 * 64 * sizeof(unsigned))) != cudaSuccess ||
+        (e = vt::dev_alloc(&bm->d_atlas, (size_t)kModels * 512 * sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMemset(bm->d_chunks, 0, 64 * 64 * 64 * sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMemset(bm->d_atlas, 0, (size_t)kModels * 512 * sizeof(unsigned))) != cudaSuccess) {
         free_brickmap(bm);
@@ -449,12 +449,12 @@ vt_status vt_brickmap_upload(vt_brickmap* bm, const uint32_t* h_chunks, const ui
     if (nbricks > (1u << 24)) return fail(bm->ctx, VT_ERR_ARG, "brick pool larger than 2^24 bricks");
     VT_CUDA(bm->ctx, cudaMemcpy(bm->d_chunks, h_chunks, 64 * 64 * 64 * sizeof(unsigned), cudaMemcpyHostToDevice));
     if (bm->d_data) {
-        cudaFree(bm->d_data);
+        vt::dev_free(bm->d_data);
         bm->d_data = nullptr;
         bm->nbricks = 0;
     }
     if (nbricks) {
-        VT_CUDA(bm->ctx, cudaMalloc(&bm->d_data, nbricks * 512 * sizeof(unsigned)));
+        VT_CUDA(bm->ctx, vt::dev_alloc(&bm->d_data, nbricks * 512 * sizeof(unsigned)));
         VT_CUDA(bm->ctx, cudaMemcpy(bm->d_data, h_bricks, nbricks * 512 * sizeof(unsigned), cudaMemcpyHostToDevice));
     }
     bm->nbricks = nbricks;

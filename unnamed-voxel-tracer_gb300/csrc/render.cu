@@ -381,12 +381,12 @@ vt_status screen_table(vt_ctx* ctx, const FrameParams& f, cudaStream_t st, bool 
     t.height = f.height;
     t.tan_half_fov = f.tan_half_fov;
     const size_t n = (size_t)f.width + (size_t)f.height;
-    VT_CUDA(ctx, cudaMalloc(&t.d, n * sizeof(float4)));
+    VT_CUDA(ctx, vt::dev_alloc(&t.d, n * sizeof(float4)));
     k_screen_table<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, st>>>(f, t.d);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
-        cudaFree(t.d);
+        vt::dev_free(t.d);
         return check_cuda(ctx, e, "screen table");
     }
     ctx->screen[ctx->n_screen++] = t;

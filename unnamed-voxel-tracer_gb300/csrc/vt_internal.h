@@ -15,9 +15,8 @@ constexpr int kBrick = 4;           // brick edge in voxels
 constexpr int kBricksPerChunk = 512;
 constexpr int kChunkBytes = kChunk * kChunk * kChunk;
 
-// Error bits of the device status word.
+// Error bit of the device status word (the checked kernels' index checks).
 constexpr unsigned kStatusOob = 1u;
-constexpr unsigned kStatusTimeout = 2u;
 
 // Device counters written by the instrumented kernels (order = vt_stats).
 constexpr int kNumCounters = 12;
@@ -178,6 +177,20 @@ struct vt_world {
 };
 
 namespace vt {
+// Every device and pinned-host allocation of the library goes through these
+// (the testing hooks vt_debug_fail_alloc / vt_debug_alloc_counts see them):
+// a failure injected by the hook reads as cudaErrorMemoryAllocation.
+cudaError_t dev_alloc_raw(void** p, size_t bytes);
+cudaError_t host_alloc_raw(void** p, size_t bytes);
+cudaError_t dev_free(void* p);
+cudaError_t host_free(void* p);
+template <class T>
+inline cudaError_t dev_alloc(T** p, size_t bytes) { return dev_alloc_raw(reinterpret_cast<void**>(p), bytes); }
+template <class T>
+inline cudaError_t host_alloc(T** p, size_t bytes) { return host_alloc_raw(reinterpret_cast<void**>(p), bytes); }
+// Looks up, once per device, the device address of vt_render_host_static's
+// fixed staging array (render_static.cu); called by vt_ctx_create.
+vt_status static_staging_init(vt_ctx* ctx);
 // Records `msg` (plus the CUDA error text when err != cudaSuccess) in the
 // context and returns the matching status.
 vt_status fail(vt_ctx* ctx, vt_status s, const std::string& msg, cudaError_t err = cudaSuccess);

@@ -274,28 +274,28 @@ vt_status world_stage(vt_world* w, size_t bytes, unsigned char** out) {
     }
     if (w->d_stage) {
         VT_CUDA(w->ctx, cudaDeviceSynchronize());
-        cudaFree(w->d_stage);
+        vt::dev_free(w->d_stage);
         w->d_stage = nullptr;
         w->stage_bytes = 0;
     }
-    VT_CUDA(w->ctx, cudaMalloc(&w->d_stage, bytes));
+    VT_CUDA(w->ctx, vt::dev_alloc(&w->d_stage, bytes));
     w->stage_bytes = bytes;
     *out = w->d_stage;
     return VT_OK;
 }
 
 static void free_world(vt_world* w) {
-    if (w->d_mask) cudaFree(w->d_mask);
-    if (w->d_mats) cudaFree(w->d_mats);
-    if (w->d_coarse) cudaFree(w->d_coarse);
-    if (w->d_palette) cudaFree(w->d_palette);
-    if (w->d_stage) cudaFree(w->d_stage);
-    if (w->d_bdist) cudaFree(w->d_bdist);
-    if (w->d_cdist) cudaFree(w->d_cdist);
-    if (w->d_dtmp) cudaFree(w->d_dtmp);
-    if (w->d_ctmp) cudaFree(w->d_ctmp);
-    if (w->d_edit) cudaFree(w->d_edit);
-    if (w->d_entities) cudaFree(w->d_entities);
+    if (w->d_mask) vt::dev_free(w->d_mask);
+    if (w->d_mats) vt::dev_free(w->d_mats);
+    if (w->d_coarse) vt::dev_free(w->d_coarse);
+    if (w->d_palette) vt::dev_free(w->d_palette);
+    if (w->d_stage) vt::dev_free(w->d_stage);
+    if (w->d_bdist) vt::dev_free(w->d_bdist);
+    if (w->d_cdist) vt::dev_free(w->d_cdist);
+    if (w->d_dtmp) vt::dev_free(w->d_dtmp);
+    if (w->d_ctmp) vt::dev_free(w->d_ctmp);
+    if (w->d_edit) vt::dev_free(w->d_edit);
+    if (w->d_entities) vt::dev_free(w->d_entities);
     delete w;
 }
 
@@ -325,16 +325,16 @@ vt_status vt_world_create(vt_ctx* ctx, const vt_world_desc* desc, vt_world** out
     w->nchunks = (size_t)w->cdim[0] * w->cdim[1] * w->cdim[2];
     w->ncoarse = (w->nchunks + 63) / 64;
     cudaError_t e;
-    if ((e = cudaMalloc(&w->d_mask, w->nchunks * kBricksPerChunk * 8)) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_mats, w->nchunks * (size_t)kChunkBytes)) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_coarse, w->ncoarse * 8)) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_palette, 256 * sizeof(unsigned))) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_bdist, kOctants * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_cdist, kOctants * (size_t)cdist_stride((unsigned)w->nchunks))) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_dtmp, 6 * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_ctmp, 6 * (size_t)cdist_stride((unsigned)w->nchunks))) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_edit, 4 * sizeof(int))) != cudaSuccess ||
-        (e = cudaMalloc(&w->d_entities, kMaxEntities * 6 * sizeof(float))) != cudaSuccess ||
+    if ((e = vt::dev_alloc(&w->d_mask, w->nchunks * kBricksPerChunk * 8)) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_mats, w->nchunks * (size_t)kChunkBytes)) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_coarse, w->ncoarse * 8)) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_palette, 256 * sizeof(unsigned))) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_bdist, kOctants * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_cdist, kOctants * (size_t)cdist_stride((unsigned)w->nchunks))) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_dtmp, 6 * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_ctmp, 6 * (size_t)cdist_stride((unsigned)w->nchunks))) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_edit, 4 * sizeof(int))) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_entities, kMaxEntities * 6 * sizeof(float))) != cudaSuccess ||
         (e = cudaMemset(w->d_edit, 0, 4 * sizeof(int))) != cudaSuccess ||
         (e = cudaMemset(w->d_mask, 0, w->nchunks * kBricksPerChunk * 8)) != cudaSuccess ||
         (e = cudaMemset(w->d_mats, 0, w->nchunks * (size_t)kChunkBytes)) != cudaSuccess ||

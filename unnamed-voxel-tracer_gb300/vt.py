@@ -106,6 +106,9 @@ _SIGNATURES = {
     "vt_ctx_destroy": (_S, [_P]),
     "vt_last_error_string": (C.c_char_p, [_P]),
     "vt_sync": (_S, [_P, _P]),
+    "vt_wait": (_S, [_P, _P, C.c_int64]),
+    "vt_debug_fail_alloc": (None, [C.c_int64]),
+    "vt_debug_alloc_counts": (None, [C.POINTER(C.c_uint64), C.POINTER(C.c_int64)]),
     "vt_device_info": (_S, [_P, C.c_char_p, C.c_int32, C.POINTER(C.c_int32)]),
     "vt_device_alloc": (_S, [_P, C.c_size_t, C.POINTER(_P)]),
     "vt_device_free": (_S, [_P, _P]),
@@ -238,6 +241,15 @@ class Context:
 
     def sync(self, stream=None) -> None:
         self.check(self.lib.vt_sync(self.handle, stream))
+
+    def wait(self, timeout_us: int, stream=None) -> bool:
+        """vt_wait: True once `stream` is done (device status checked), False
+        if it is still busy after timeout_us microseconds."""
+        st = self.lib.vt_wait(self.handle, stream, int(timeout_us))
+        if st == 5:   # VT_ERR_TIMEOUT
+            return False
+        self.check(st)
+        return True
 
     def set_tuning(self, kernel: int = KERNEL_TILE, warp_tile_w: int = 8, occupancy: int = 1,
                    batch: int = 16) -> None:
@@ -434,6 +446,18 @@ class Camera:
         pos = (C.c_float * 3)(*self.pos)
         _check(lib.vt_camera_look(pos, self.yaw, self.pitch, self.fov, self.width, self.height, C.byref(cam)))
         return cam
+
+
+def fail_alloc(n: int) -> None:
+    """Testing hook: the n-th next allocation of the library fails (0 disarms)."""
+    load().vt_debug_fail_alloc(int(n))
+
+
+def alloc_counts() -> tuple[int, int]:
+    """(allocations made, allocations live) by the library, process-wide."""
+    made, live = C.c_uint64(), C.c_int64()
+    load().vt_debug_alloc_counts(C.byref(made), C.byref(live))
+    return made.value, live.value
 
 
 def default_params(**kw) -> Params_t:
