@@ -448,6 +448,15 @@ vt_status vt_get_tuning(vt_ctx* ctx, vt_tuning* tuning);
 vt_status vt_autotune(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, const vt_params* params,
                       int32_t reps, const char* cache_path, vt_tuning* best, float* best_ms);
 
+/* No counterpart in the reference: a measurement aid for roofline
+ * denominators.  Streams a device buffer of `bytes` (allocated and freed by
+ * this call) `passes` times in one launch of a read kernel with 16-byte
+ * L2-only loads; *gbs = bytes * passes / that launch's time (CUDA events on
+ * the context's stream, after one warm-up launch).  A buffer that fits in L2
+ * (a few tens of MiB on GB300) gives the L2 read bandwidth; one far larger
+ * than L2 the HBM read bandwidth.  Synchronous. */
+vt_status vt_probe_read_bandwidth(vt_ctx* ctx, uint64_t bytes, int32_t passes, float* gbs);
+
 /* traceMap over an explicit ray list (map.glsl:83-168 semantics on the mode-P
  * world, no clipping beyond the grid box): d_origins/d_dirs are n*3 floats. */
 vt_status vt_trace_rays(vt_ctx* ctx, const vt_world* world, const float* d_origins,

@@ -85,8 +85,76 @@ def load() -> C.CDLL:
                                    C.c_int32, C.POINTER(VtoRefHit_t)]
         lib.vto_pick_p.argtypes = [C.POINTER(VtoWorld_t), C.POINTER(vt.Camera_t), C.c_int32, C.c_int32,
                                    C.POINTER(VtoTrace_t), C.POINTER(C.c_int32)]
+        G = C.POINTER(vt.GenDesc_t)
+        lib.vto_gen_desc_init.argtypes = [G, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64]
+        lib.vto_gen_desc_init.restype = None
+        lib.vto_gen_world.argtypes = [G, P, C.c_size_t, C.c_int32]
+        lib.vto_gen_world.restype = C.c_int32
+        lib.vto_gen_height.argtypes = [G, C.c_int32, C.c_int32]
+        lib.vto_gen_height.restype = C.c_int32
+        lib.vto_gen_camera.argtypes = [G, C.c_uint64, C.c_int32, C.c_int32, C.POINTER(vt.Camera_t)]
+        lib.vto_gen_camera.restype = C.c_int32
+        lib.vto_default_palette.argtypes = [P]
+        lib.vto_default_palette.restype = None
+        lib.vto_gen_sun.argtypes = [C.c_uint64, C.POINTER(C.c_float)]
+        lib.vto_gen_sun.restype = None
         _lib = lib
     return _lib
+
+
+# ------------------------------------------------ seeded scenes (vt_oracle_gen.c)
+# The same scenes as the library's vt.gen_* helpers, without loading libvt.so.
+def gen_desc(dims, scale: float = 1.0, seed: int = 0, trees: int = 0, caves: bool = False):
+    d = vt.GenDesc_t()
+    load().vto_gen_desc_init(C.byref(d), int(dims[0]), int(dims[1]), int(dims[2]), float(scale), int(seed))
+    d.trees = int(trees)
+    d.caves = 1 if caves else 0
+    return d
+
+
+def gen_world(desc, threads: int = 0) -> np.ndarray:
+    X, Y, Z = desc.dims
+    out = np.zeros((Z, Y, X), dtype=np.uint8)
+    import os
+    if load().vto_gen_world(C.byref(desc), out.ctypes.data, out.nbytes, threads or (os.cpu_count() or 1)) != 0:
+        raise ValueError("bad generator description")
+    return out
+
+
+def gen_camera(desc, seed: int, width: int, height: int):
+    cam = vt.Camera_t()
+    if load().vto_gen_camera(C.byref(desc), int(seed), int(width), int(height), C.byref(cam)) != 0:
+        raise ValueError("bad camera arguments")
+    return cam
+
+
+def gen_sun(seed: int):
+    out = (C.c_float * 3)()
+    load().vto_gen_sun(int(seed), out)
+    return [float(v) for v in out]
+
+
+def default_palette() -> np.ndarray:
+    pal = np.zeros(256, np.uint32)
+    load().vto_default_palette(pal.ctypes.data)
+    return pal
+
+
+def default_params(**kw):
+    """vt_params_default's values (the reference's SUN_DIR, camera.glsl:8), as
+    a vt.Params_t, with fields overridden by keyword."""
+    p = vt.Params_t()
+    p.max_steps, p.shadow_max_steps, p.bounce_max_steps = 512, 512, 256
+    p.rays, p.shade, p.flags, p.seed = vt.RAYS_PRIMARY | vt.RAYS_SHADOW, vt.SHADE_REFERENCE, \
+        vt.FLAG_CROSSHAIR | vt.FLAG_VIGNETTE, 0
+    p.sun_dir = (C.c_float * 3)(7.52185881e-01, 6.58950984e-01, 7.52185881e-01)
+    p.ambient, p.diffuse, p.bounce_weight = 0.2, 0.8, 0.3
+    for k, v in kw.items():
+        if k == "sun_dir":
+            p.sun_dir = (C.c_float * 3)(*v)
+        else:
+            setattr(p, k, v)
+    return p
 
 
 class OracleWorld:

@@ -144,6 +144,18 @@ void vto_sky_ref(const float rd[3], float out[4]);
 void vto_render_reference(const vto_refworld* w, const float cam_pos[4], const float view[16], float fov,
                           int32_t width, int32_t height, vt_ref_pixel* out);
 
+/* ------------------------------------------------------ seeded scenes
+ * vt_oracle_gen.c: the benchmark's synthetic scenes, the same bytes as the
+ * library's host generator (vt_gen_*), for runs that must not load it. */
+void    vto_gen_desc_init(vt_gen_desc* d, int32_t x, int32_t y, int32_t z, float scale, uint64_t seed);
+int32_t vto_gen_world(const vt_gen_desc* d, uint8_t* out, size_t nbytes, int32_t threads);
+int32_t vto_gen_height(const vt_gen_desc* d, int32_t x, int32_t z);
+int32_t vto_camera_look(const float pos[3], float yaw, float pitch, float fov, int32_t width, int32_t height,
+                        vt_camera* out);
+int32_t vto_gen_camera(const vt_gen_desc* d, uint64_t seed, int32_t width, int32_t height, vt_camera* out);
+void    vto_default_palette(uint32_t pal[256]);
+void    vto_gen_sun(uint64_t seed, float out[3]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -57,11 +57,74 @@ void cache_store(const char* path, const std::string& key, const vt_tuning& t, f
     out << key << ' ' << t.kernel << ' ' << t.warp_tile_w << ' ' << t.occupancy << ' ' << t.batch << ' ' << ms << '\n';
 }
 
+// Read-bandwidth probe: each thread streams 16-byte words of the buffer with
+// L2-only loads (ld.global.cg, so that no pass is served from L1), four
+// independent loads in flight per turn, `passes` times in one launch.  The
+// XOR of everything read is kept live by a store that never happens.
+constexpr int kProbeBlock = 512;
+__global__ void __launch_bounds__(kProbeBlock) k_read_probe(const uint4* __restrict__ buf, size_t n16, int passes,
+                                                             unsigned* __restrict__ sink) {
+    const size_t stride = (size_t)gridDim.x * kProbeBlock;
+    const size_t first = (size_t)blockIdx.x * kProbeBlock + threadIdx.x;
+    unsigned acc = 0;
+    for (int p = 0; p < passes; ++p) {
+        size_t i = first;
+        for (; i + 3 * stride < n16; i += 4 * stride) {
+            const uint4 a = __ldcg(buf + i), b = __ldcg(buf + i + stride), c = __ldcg(buf + i + 2 * stride),
+                        d = __ldcg(buf + i + 3 * stride);
+            acc ^= (a.x ^ a.y ^ a.z ^ a.w) ^ (b.x ^ b.y ^ b.z ^ b.w) ^ (c.x ^ c.y ^ c.z ^ c.w) ^ (d.x ^ d.y ^ d.z ^ d.w);
+        }
+        for (; i < n16; i += stride) {
+            const uint4 a = __ldcg(buf + i);
+            acc ^= a.x ^ a.y ^ a.z ^ a.w;
+        }
+        acc = acc * 0x9E3779B1u + (unsigned)p;   // passes stay distinct work
+    }
+    if (acc == 0x2545F491u) atomicAdd(sink, 1u);
+}
+
 }  // namespace
 
 using namespace vt;
 
 extern "C" {
+
+vt_status vt_probe_read_bandwidth(vt_ctx* ctx, uint64_t bytes, int32_t passes, float* gbs) {
+    if (!ctx) return VT_ERR_ARG;
+    if (!gbs || passes < 1 || passes > 100000 || bytes < (1u << 20) || bytes > (64ull << 30) || bytes % 16)
+        return fail(ctx, VT_ERR_ARG, "probe: bytes in [1 MiB, 64 GiB], a multiple of 16; passes in [1, 100000]");
+    void* buf = nullptr;
+    unsigned* sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = dev_alloc(&buf, (size_t)bytes);
+    if (e == cudaSuccess) e = dev_alloc(&sink, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemsetAsync(buf, 0x5A, (size_t)bytes, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) {
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_read_probe, kProbeBlock, 0);
+        const unsigned blocks = (unsigned)(ctx->sm_count * (per_sm > 0 ? per_sm : 1));
+        const size_t n16 = (size_t)bytes / 16;
+        if (e == cudaSuccess) {
+            k_read_probe<<<blocks, kProbeBlock, 0, ctx->stream>>>((const uint4*)buf, n16, 1, sink);  // warm-up
+            cudaEventRecord(e0, ctx->stream);
+            k_read_probe<<<blocks, kProbeBlock, 0, ctx->stream>>>((const uint4*)buf, n16, passes, sink);
+            cudaEventRecord(e1, ctx->stream);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    dev_free(sink);
+    dev_free(buf);
+    if (e != cudaSuccess) return check_cuda(ctx, e, "read-bandwidth probe");
+    *gbs = (float)((double)bytes * (double)passes / ((double)ms * 1e-3) / 1e9);
+    return VT_OK;
+}
 
 vt_status vt_set_tuning(vt_ctx* ctx, const vt_tuning* t) {
     if (!ctx) return VT_ERR_ARG;

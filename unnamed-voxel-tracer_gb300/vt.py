@@ -160,6 +160,7 @@ _SIGNATURES = {
     "vt_batch_launch": (_S, [_P, _P]),
     "vt_batch_destroy": (_S, [_P]),
     "vt_batch_info": (_S, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_int32), C.POINTER(C.c_uint32)]),
+    "vt_probe_read_bandwidth": (_S, [_P, C.c_uint64, C.c_int32, C.POINTER(C.c_float)]),
     "vt_set_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
     "vt_get_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
     "vt_autotune": (_S, [_P, _P, C.POINTER(Camera_t), C.POINTER(Params_t), C.c_int32, C.c_char_p,
@@ -268,6 +269,12 @@ class Context:
         self.check(self.lib.vt_autotune(self.handle, world.handle, C.byref(cam), C.byref(params), reps,
                                         cache_path.encode() if cache_path else None, C.byref(t), C.byref(ms)))
         return t.as_dict(), float(ms.value)
+
+    def read_bandwidth(self, nbytes: int, passes: int) -> float:
+        """GB/s of the library's read probe over a buffer of nbytes, passes times."""
+        g = C.c_float()
+        self.check(self.lib.vt_probe_read_bandwidth(self.handle, int(nbytes), int(passes), C.byref(g)))
+        return g.value
 
     def device_info(self) -> tuple[str, int]:
         buf = C.create_string_buffer(256)
