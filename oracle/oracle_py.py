@@ -85,6 +85,8 @@ def load() -> C.CDLL:
                                    C.c_int32, C.POINTER(VtoRefHit_t)]
         lib.vto_pick_p.argtypes = [C.POINTER(VtoWorld_t), C.POINTER(vt.Camera_t), C.c_int32, C.c_int32,
                                    C.POINTER(VtoTrace_t), C.POINTER(C.c_int32)]
+        lib.vto_primary_rays.argtypes = [C.POINTER(vt.Camera_t), C.c_int32, P, P]
+        lib.vto_primary_rays.restype = None
         G = C.POINTER(vt.GenDesc_t)
         lib.vto_gen_desc_init.argtypes = [G, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64]
         lib.vto_gen_desc_init.restype = None
@@ -100,6 +102,15 @@ def load() -> C.CDLL:
         lib.vto_gen_sun.restype = None
         _lib = lib
     return _lib
+
+
+def primary_rays(cam, row_step: int = 1):
+    """(origins, dirs) of the primary rays of every row_step-th row, (n, 3) float32."""
+    rows = (cam.height + row_step - 1) // row_step
+    o = np.zeros((rows * cam.width, 3), np.float32)
+    d = np.zeros((rows * cam.width, 3), np.float32)
+    load().vto_primary_rays(C.byref(cam), int(row_step), o.ctypes.data, d.ctypes.data)
+    return o, d
 
 
 # ------------------------------------------------ seeded scenes (vt_oracle_gen.c)

@@ -496,6 +496,13 @@ static void shade_pixel(const vto_world* w, const uint32_t* palette, const vt_ca
     *out = h;
 }
 
+void vto_primary_rays(const vt_camera* cam, int32_t row_step, float* origins, float* dirs) {
+    if (row_step < 1) row_step = 1;
+    size_t k = 0;
+    for (int py = 0; py < cam->height; py += row_step)
+        for (int px = 0; px < cam->width; ++px, ++k) primary_ray(cam, px, py, origins + 3 * k, dirs + 3 * k);
+}
+
 void vto_render_rows(const vto_world* w, const uint32_t* palette, const vt_camera* cam,
                      const vt_params* p, vt_hit* out, int32_t y0, int32_t y1, vt_stats* st) {
     for (int32_t y = y0; y < y1; ++y)

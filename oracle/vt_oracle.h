@@ -144,6 +144,10 @@ void vto_sky_ref(const float rd[3], float out[4]);
 void vto_render_reference(const vto_refworld* w, const float cam_pos[4], const float view[16], float fov,
                           int32_t width, int32_t height, vt_ref_pixel* out);
 
+/* The primary rays of every row_step-th row of a frame (row-major), as the
+ * render path makes them: origins and dirs get 3 floats per ray. */
+void vto_primary_rays(const vt_camera* cam, int32_t row_step, float* origins, float* dirs);
+
 /* ------------------------------------------------------ seeded scenes
  * vt_oracle_gen.c: the benchmark's synthetic scenes, the same bytes as the
  * library's host generator (vt_gen_*), for runs that must not load it. */

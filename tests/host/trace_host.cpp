@@ -1,11 +1,14 @@
 // Test-only: compiles the device traversal (trace_p.cuh) as host C++ so that
-// its jump logic can be compared with the unit-step oracle without a GPU.
-// The CUDA intrinsics it uses are given their IEEE host equivalents.
+// its jump logic can be compared with the unit-step oracle without a GPU, and
+// so that the benchmark can time the skipping walk on the host cores beside
+// the unit-step oracle (ht_world_new / ht_trace_mt).  The CUDA intrinsics it
+// uses are given their IEEE host equivalents.
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
 #include <limits.h>
 #include <algorithm>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -122,6 +125,145 @@ extern "C" void ht_distances(const int32_t dims[3], const uint8_t* dense, uint8_
     distances(cd, mask, b, c, nch);
     std::copy(b.begin(), b.end(), h_brick);
     std::copy(c.begin(), c.end(), h_chunk);
+}
+
+// A mode-P world in the kernel's layout (brick words, materials, coarse bits,
+// octant distances), built once on the host.
+struct HostWorld {
+    vt::WorldView w;
+    std::vector<unsigned long long> mask, coarse;
+    std::vector<unsigned char> mats, bdist, cdist;
+};
+
+extern "C" void* ht_world_new(const int32_t dims[3], const uint8_t* dense) {
+    HostWorld* hw = new HostWorld();
+    vt::WorldView& w = hw->w;
+    memset(&w, 0, sizeof(w));
+    int cd[3];
+    for (int i = 0; i < 3; ++i) {
+        w.dims[i] = dims[i];
+        cd[i] = w.cdim[i] = (dims[i] + 31) / 32;
+    }
+    const size_t nch = (size_t)cd[0] * cd[1] * cd[2];
+    hw->mask.assign(nch * 512, 0ull);
+    hw->coarse.assign((nch + 63) / 64, 0ull);
+    hw->mats.assign(nch * 32768, 0);
+    for (int z = 0; z < dims[2]; ++z)
+        for (int y = 0; y < dims[1]; ++y)
+            for (int x = 0; x < dims[0]; ++x) {
+                unsigned char m = dense[(size_t)x + (size_t)dims[0] * ((size_t)y + (size_t)dims[1] * z)];
+                if (!m) continue;
+                size_t ci = (size_t)(x >> 5) + cd[0] * ((size_t)(y >> 5) + (size_t)cd[1] * (z >> 5));
+                unsigned bi = ((x >> 2) & 7) | (((y >> 2) & 7) << 3) | (((z >> 2) & 7) << 6);
+                unsigned vb = (x & 3) | ((y & 3) << 2) | ((z & 3) << 4);
+                hw->mask[ci * 512 + bi] |= 1ull << vb;
+                hw->mats[(ci * 512 + bi) * 64 + vb] = m;
+                hw->coarse[ci >> 6] |= 1ull << (ci & 63);
+            }
+    const unsigned cstride = vt::cdist_stride((unsigned)nch);
+    distances(cd, hw->mask, hw->bdist, hw->cdist, cstride);
+    w.mask = hw->mask.data();
+    w.mats = hw->mats.data();
+    w.coarse = hw->coarse.data();
+    w.bdist = hw->bdist.data();
+    w.cdist = hw->cdist.data();
+    w.nwords = (unsigned)(nch * 512);
+    w.ncoarse = (unsigned)hw->coarse.size();
+    w.nchunks = (unsigned)nch;
+    w.cstride = cstride;
+    return hw;
+}
+
+extern "C" void ht_world_free(void* p) { delete static_cast<HostWorld*>(p); }
+
+// The production walk over n rays on `threads` host threads (rays split in
+// interleaved blocks of 256): out gets per ray {voxel, t bits, material,
+// face | hit << 8} (voxel 0xFFFFFFFF on a miss).
+extern "C" void ht_trace_mt(const void* world, const float* origins, const float* dirs, int64_t n, int32_t max_steps,
+                            uint32_t* out, int32_t threads) {
+    const vt::WorldView& w = static_cast<const HostWorld*>(world)->w;
+    auto work = [&](int t) {
+        for (int64_t b = (int64_t)t * 256; b < n; b += (int64_t)threads * 256) {
+            const int64_t e = std::min<int64_t>(n, b + 256);
+            for (int64_t i = b; i < e; ++i) {
+                vt::PRay r;
+                vt::pray_init(r, origins + 3 * i, dirs + 3 * i);
+                vt::TraceHit h;
+                const bool hit = vt::near_origin(r.o) ? vt::trace_fast<true, true, true>(w, w.cdist, r, max_steps, h)
+                                                      : vt::trace_fast<true, true, false>(w, w.cdist, r, max_steps, h);
+                uint32_t* o = out + 4 * i;
+                if (hit) {
+                    o[0] = (uint32_t)h.c[0] + (uint32_t)w.dims[0] * ((uint32_t)h.c[1] + (uint32_t)w.dims[1] * (uint32_t)h.c[2]);
+                    memcpy(&o[1], &h.t, 4);
+                    o[2] = h.mat;
+                    o[3] = (2u * h.axis + (r.pos[h.axis] ? 0u : 1u)) | (1u << 8);
+                } else {
+                    const float mt = -1.0f;
+                    o[0] = 0xFFFFFFFFu;
+                    memcpy(&o[1], &mt, 4);
+                    o[2] = 0;
+                    o[3] = 0xFFu;
+                }
+            }
+        }
+    };
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto& th : pool) th.join();
+}
+
+// One frame's rays on `threads` host threads: the primary ray of each entry
+// (origins/dirs), and for each hit the shadow ray toward sun (origin = the hit
+// point moved 0.001 off the entered face, as in the render kernel).  Returns
+// the rays traced; *shadowed counts the blocked shadow rays.
+extern "C" int64_t ht_frame_mt(const void* world, const float* origins, const float* dirs, int64_t n,
+                               int32_t max_steps, const float sun[3], int32_t shadow_max_steps, int32_t threads,
+                               int64_t* shadowed) {
+    const vt::WorldView& w = static_cast<const HostWorld*>(world)->w;
+    float sd[3], sinv[3];
+    for (int j = 0; j < 3; ++j) {
+        sd[j] = sun[j] == 0.0f ? 0.001f : sun[j];
+        sinv[j] = 1.0f / sd[j];
+    }
+    if (threads < 1) threads = 1;
+    std::vector<int64_t> rays(threads, 0), dark(threads, 0);
+    auto work = [&](int t) {
+        for (int64_t b = (int64_t)t * 256; b < n; b += (int64_t)threads * 256) {
+            const int64_t e = std::min<int64_t>(n, b + 256);
+            for (int64_t i = b; i < e; ++i) {
+                vt::PRay r;
+                vt::pray_init(r, origins + 3 * i, dirs + 3 * i);
+                vt::TraceHit h;
+                rays[t]++;
+                const bool hit = vt::near_origin(r.o) ? vt::trace_fast<true, true, true>(w, w.cdist, r, max_steps, h)
+                                                      : vt::trace_fast<true, true, false>(w, w.cdist, r, max_steps, h);
+                if (!hit || shadow_max_steps <= 0) continue;
+                float so[3];
+                for (int j = 0; j < 3; ++j) {
+                    so[j] = fmaf(r.d[j], h.t, origins[3 * i + j]);
+                    if (j == h.axis) so[j] = so[j] + (r.pos[j] ? -1.0f : 1.0f) * 0.001f;
+                }
+                vt::PRay rs;
+                vt::pray_init_dir(rs, so, sd, sinv);
+                vt::TraceHit hs;
+                rays[t]++;
+                dark[t] += vt::trace_fast<false, true, true>(w, w.cdist, rs, shadow_max_steps, hs) ? 1 : 0;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto& th : pool) th.join();
+    int64_t total = 0, blocked = 0;
+    for (int t = 0; t < threads; ++t) {
+        total += rays[t];
+        blocked += dark[t];
+    }
+    if (shadowed) *shadowed = blocked;
+    return total;
 }
 
 extern "C" int ht_trace_rays(const int32_t dims[3], const uint8_t* dense, const float* origins, const float* dirs,

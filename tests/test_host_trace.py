@@ -30,7 +30,7 @@ def cuda_include():
 def ht():
     if not OUT.exists() or any(d.stat().st_mtime > OUT.stat().st_mtime for d in DEPS):
         OUT.parent.mkdir(exist_ok=True)
-        subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", cuda_include(),
+        subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-I", cuda_include(),
                         str(SRC), "-o", str(OUT)], check=True)
     lib = C.CDLL(str(OUT))
     lib.ht_trace_rays.restype = C.c_int
@@ -132,3 +132,42 @@ def test_counters_match_oracle(ht, oracle, vtlib):
         mw += tr.mask_words
         cw += tr.coarse_words
     assert (int(cnt[0]), int(cnt[1])) == (mw, cw)
+
+
+def test_threaded_frame_tracer_matches_oracle(ht, oracle, vtlib):
+    """The benchmark's CPU leg for the skipping walk (ht_world_new, ht_trace_mt,
+    ht_frame_mt on several threads) against the unit-step oracle: the same
+    primary records, and the same primary + shadow ray and blocked counts."""
+    ht.ht_world_new.restype = C.c_void_p
+    ht.ht_world_new.argtypes = [C.POINTER(C.c_int32), C.c_void_p]
+    ht.ht_world_free.argtypes = [C.c_void_p]
+    ht.ht_trace_mt.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int32]
+    ht.ht_frame_mt.restype = C.c_int64
+    ht.ht_frame_mt.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_float),
+                               C.c_int32, C.c_int32, C.POINTER(C.c_int64)]
+    d = oracle.gen_desc((160, 96, 128), seed=4, trees=20)
+    mats = oracle.gen_world(d)
+    cam = oracle.gen_camera(d, 2, 120, 80)
+    sun = oracle.gen_sun(4)
+    p = oracle.default_params(rays=vtlib.RAYS_PRIMARY | vtlib.RAYS_SHADOW, sun_dir=sun)
+    Z, Y, X = mats.shape
+    hw = ht.ht_world_new((C.c_int32 * 3)(X, Y, Z), mats.ctypes.data)
+    try:
+        o, dd = oracle.primary_rays(cam)
+        n = o.shape[0]
+        out = np.zeros(n * 4, np.uint32)
+        ht.ht_trace_mt(hw, o.ctypes.data, dd.ctypes.data, n, 512, out.ctypes.data, 3)
+        recs, st = oracle.render(oracle.OracleWorld(mats), oracle.default_palette(), cam, p, threads=2)
+        out = out.reshape(n, 4)
+        assert np.array_equal(out[:, 0], recs["voxel"])
+        assert np.array_equal(out[:, 1], recs["t"].view(np.uint32))
+        hitm = out[:, 0] != 0xFFFFFFFF
+        assert np.array_equal(out[hitm, 2], recs["material"][hitm])
+        assert np.array_equal(out[hitm, 3] & 0xFF, recs["face"][hitm])
+        dark = C.c_int64()
+        rays = ht.ht_frame_mt(hw, o.ctypes.data, dd.ctypes.data, n, 512, (C.c_float * 3)(*sun), 512, 4,
+                              C.byref(dark))
+        assert rays == st["primary_rays"] + st["shadow_rays"]
+        assert dark.value == st["shadow_hits"] and st["shadow_hits"] > 100
+    finally:
+        ht.ht_world_free(hw)
