@@ -374,36 +374,37 @@ def measure_config2(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py) -
                              "sample": "camera 0: " + dsc}}
 
 
-def launch_floor(torch, n: int, chains: int) -> dict:
-    """Fixed costs of the launch structures, measured with trivial kernels: n
-    one-element launches back to back on one stream, and the same n launches
-    as a CUDA graph on `chains` concurrent chains, replayed."""
-    x = torch.zeros(chains, device="cuda")
-    one = _timed(torch, lambda: [x[:1].add_(1.0) for _ in range(n)], 5)
-    streams = [torch.cuda.Stream() for _ in range(chains)]
-    g = torch.cuda.CUDAGraph()
-    cap = torch.cuda.Stream()
-    cap.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(cap):
-        with torch.cuda.graph(g, stream=cap):
-            cur = torch.cuda.current_stream()
-            for s in streams:
-                s.wait_stream(cur)
-            for j in range(n):
-                with torch.cuda.stream(streams[j % chains]):
-                    x[j % chains:j % chains + 1].add_(1.0)
-            for s in streams:
-                cur.wait_stream(s)
-    torch.cuda.synchronize()
-    graph = _timed(torch, g.replay, 20)
-    return {"trivial_launches_one_stream_ms": one, "trivial_graph_ms": graph, "launches": n, "chains": chains}
+def launch_floor(torch, n: int) -> dict:
+    """Fixed costs of the launch structures, measured with trivial kernels
+    (one-element adds) in CUDA graphs: n launches in sequence on one chain,
+    and n launches spread over 8 concurrent chains."""
+    def graph_of(chains: int) -> float:
+        x = torch.zeros(chains, device="cuda")
+        streams = [torch.cuda.Stream() for _ in range(chains)]
+        g = torch.cuda.CUDAGraph()
+        cap = torch.cuda.Stream()
+        cap.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(cap):
+            with torch.cuda.graph(g, stream=cap):
+                cur = torch.cuda.current_stream()
+                for s in streams:
+                    s.wait_stream(cur)
+                for j in range(n):
+                    with torch.cuda.stream(streams[j % chains]):
+                        x[j % chains:j % chains + 1].add_(1.0)
+                for s in streams:
+                    cur.wait_stream(s)
+        torch.cuda.synchronize()
+        return _timed(torch, g.replay, 20)
+    return {"trivial_graph_one_chain_ms": graph_of(1), "trivial_graph_8_chains_ms": graph_of(8), "launches": n}
 
 
 def measure_config3(vt, scenes, ctx, torch, peak, peak_kind, oracle_py) -> dict:
     """64 cube scenes (edge log-uniform in [32, 512]) x 1-8 cameras: one
     CUDA-graph launch of the batch vs one vt_render launch per camera.  The
-    default batch graph holds the per-camera launches on 8 concurrent chains;
-    the queue shape (one persistent kernel over 16x16 units) is timed too."""
+    default batch graph holds one launch per chunk of up to 104 jobs; the
+    per-job shape (one launch per camera on 8 concurrent chains) and the
+    queue shape (one persistent kernel over 16x16 units) are timed too."""
     sc, params = scenes.config3()
     worlds, jobs = [], []
     for desc, cams in sc:
@@ -418,25 +419,27 @@ def measure_config3(vt, scenes, ctx, torch, peak, peak_kind, oracle_py) -> dict:
         for w, c, buf in jobs:
             ctx.check(ctx.lib.vt_render(ctx.handle, w.handle, C.byref(c), C.byref(params), buf.ptr, sh))
 
-    batch = vt.Batch(ctx, jobs, params)
+    def shape_ms(kernel: int) -> float:
+        ctx.set_tuning(kernel=kernel)
+        b = vt.Batch(ctx, jobs, params)
+        b.launch(sh)                     # captured with this tuning
+        ctx.set_tuning()
+        ms = _timed(torch, lambda: b.launch(sh), 3)
+        b.close()
+        return ms
+
     per_scene()
-    batch.launch(sh)
     t_scene = _timed(torch, per_scene, 3)
-    t_batch = _timed(torch, lambda: batch.launch(sh), 3)
-    pixels = batch.info()["pixels"]
-    batch.close()
-    ctx.set_tuning(kernel=vt.KERNEL_QUEUE)
-    qbatch = vt.Batch(ctx, jobs, params)
-    qbatch.launch(sh)
-    ctx.set_tuning()
-    t_queue = _timed(torch, lambda: qbatch.launch(sh), 3)
-    qbatch.close()
+    t_batch = shape_ms(vt.KERNEL_TILE)
+    t_per_job = shape_ms(vt.KERNEL_PER_JOB)
+    t_queue = shape_ms(vt.KERNEL_QUEUE)
+    pixels = sum(c.width * c.height for _, c, _ in jobs)
     abytes, rays = 0.0, 0
     for w, c, _ in jobs:
         s = vt.render_stats(ctx, w, c, params, sh)
         abytes += ray_bytes(s)
         rays += s["primary_rays"] + s["shadow_rays"]
-    floor = launch_floor(torch, len(jobs), 8)
+    floor = launch_floor(torch, len(jobs))
     # CPU: the oracle on sampled rows of the first jobs, about 4 s
     threads = os.cpu_count() or 1
     crays, csecs, used = 0.0, 0.0, 0
@@ -460,6 +463,7 @@ def measure_config3(vt, scenes, ctx, torch, peak, peak_kind, oracle_py) -> dict:
             "per_scene_gpix_per_s": pixels / (t_scene * 1e-3) / 1e9,
             "batched_grays_per_s": rays / (t_batch * 1e-3) / 1e9,
             "batched_ms": t_batch, "per_scene_ms": t_scene, "speedup": t_scene / t_batch,
+            "batched_per_job_gpix_per_s": pixels / (t_per_job * 1e-3) / 1e9, "batched_per_job_ms": t_per_job,
             "batched_queue_gpix_per_s": pixels / (t_queue * 1e-3) / 1e9, "batched_queue_ms": t_queue,
             "launches_per_scene_path": len(jobs), "launch_floor": floor,
             "roofline": roofline(abytes, t_batch * 1e-3, peak, peak_kind, RAY_BYTES + ", all jobs of the batch"),

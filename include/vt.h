@@ -358,10 +358,13 @@ vt_status vt_brickmap_edit(vt_ctx* ctx, vt_brickmap* bm, const vt_camera* cam, i
 /* ----------------------------------------------------------------- batch
  * Many scenes x cameras in one graph launch (no counterpart in the reference,
  * which renders one camera per frame, game.zig:232-256).  Under the default
- * tuning the graph holds one render launch per job on eight concurrent
- * chains; under VT_KERNEL_QUEUE it holds one persistent kernel that pulls
- * 16x16-pixel units of all jobs from a device work queue.  Every job's
- * records are identical to what vt_render writes for it alone. */
+ * tuning (VT_KERNEL_TILE) the graph holds one render launch per chunk of up
+ * to 104 jobs and 32 worlds, whose grid covers the 16x16-pixel tiles of all
+ * its jobs (the chunk's job table travels as the launch's parameters); under
+ * VT_KERNEL_PER_JOB it holds one render launch per job on eight concurrent
+ * chains; under VT_KERNEL_QUEUE one persistent kernel that pulls 16x16-pixel
+ * units of all jobs from a device work queue.  Every job's records are
+ * identical to what vt_render writes for it alone. */
 typedef struct {
     const vt_world* world;
     vt_camera camera;
@@ -430,8 +433,9 @@ vt_status vt_shade_backward_views(vt_ctx* ctx, const vt_world* world, int32_t n,
  * Launch configuration of the render kernels (no counterpart in the
  * reference, whose dispatch shape is fixed at 32x32 groups, game.zig:241-248).
  * Every configuration produces identical records; only speed differs. */
-#define VT_KERNEL_TILE  0 /* one thread per pixel, warp = pixel tile */
-#define VT_KERNEL_QUEUE 1 /* persistent warps refilling lanes from a pixel queue */
+#define VT_KERNEL_TILE    0 /* one thread per pixel, warp = pixel tile; a batch: one launch per chunk of jobs */
+#define VT_KERNEL_QUEUE   1 /* persistent warps refilling lanes from a pixel queue */
+#define VT_KERNEL_PER_JOB 2 /* as VT_KERNEL_TILE for single frames; a batch: one launch per job */
 typedef struct {
     int32_t kernel;       /* VT_KERNEL_* */
     int32_t warp_tile_w;  /* VT_KERNEL_TILE: a warp's tile is w x (32/w) pixels, w in {8, 16, 32} */

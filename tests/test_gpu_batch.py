@@ -1,15 +1,17 @@
 """The batched launch (vt_batch_*): many worlds of different sizes, several
-cameras each at different resolutions, one CUDA-graph launch, in both shapes
-(per-job launches on concurrent graph chains; one persistent unit-queue
-kernel).  Every job's records must equal what vt_render writes for that job
-alone (and hence the oracle's, which test_gpu_render checks for vt_render)."""
+cameras each at different resolutions, one CUDA-graph launch, in all three
+shapes (one launch per chunk of jobs with the job table as the launch's
+parameters; per-job launches on concurrent graph chains; one persistent
+unit-queue kernel).  Every job's records must equal what vt_render writes for
+that job alone (and hence the oracle's, which test_gpu_render checks for
+vt_render)."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("kernel", [0, 1], ids=["tile-graph", "queue"])
+@pytest.mark.parametrize("kernel", [0, 1, 2], ids=["chunks", "queue", "per-job"])
 def test_batch_matches_per_job_renders(vt, ctx, oracle, kernel):
     rng = np.random.default_rng(31)
     worlds, jobs, outs = [], [], []
@@ -51,9 +53,9 @@ def test_batch_matches_per_job_renders(vt, ctx, oracle, kernel):
 
 def test_batch_captured_in_a_fresh_context(vt):
     """A context that has rendered nothing yet holds no screen tables: the
-    batch graph is captured without making any (no allocation or
-    synchronisation inside a capture) and still equals the per-job renders,
-    which then make the tables."""
+    batch makes those it needs before its capture (no allocation or
+    synchronisation inside a capture) and equals the per-job renders and the
+    allocation-free entry point."""
     ctx = vt.Context(0)
     try:
         d = vt.gen_desc((96, 64, 80), scale=0.5, seed=77)
@@ -69,7 +71,7 @@ def test_batch_captured_in_a_fresh_context(vt):
         ctx.sync()
         for i, (_, cam, buf) in enumerate(jobs):
             got = buf.download(np.zeros(cam.width * cam.height, vt.HIT_DTYPE))
-            if i == 0:  # the allocation-free entry point before any table of this size exists
+            if i == 0:
                 assert np.array_equal(got, vt.render_host_static(ctx, w, cam, params))
             assert np.array_equal(got, vt.render_host(ctx, w, cam, params))
             assert np.array_equal(got, vt.render_host_static(ctx, w, cam, params))
@@ -79,3 +81,40 @@ def test_batch_captured_in_a_fresh_context(vt):
         w.close()
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("checked", [False, True], ids=["plain", "checked"])
+def test_batch_many_chunks(vt, ctx, checked):
+    """More jobs (126) and worlds (42) than one chunked launch holds (104 and
+    32): the batch spans several launches; small and ragged frames; the
+    bounds-checked variant too.  Every job equals its own vt_render."""
+    rng = np.random.default_rng(41)
+    flags = vt.FLAG_CROSSHAIR | vt.FLAG_VIGNETTE | (vt.FLAG_CHECKED if checked else 0)
+    params = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=vt.gen_sun(41), flags=flags)
+    worlds, jobs = [], []
+    try:
+        for s in range(42):
+            edge = int(rng.integers(24, 72))
+            d = vt.gen_desc((edge, edge, edge), scale=edge / 128.0, seed=900 + s)
+            w = vt.World(ctx, (edge, edge, edge))
+            w.upload_dense(vt.gen_world(d))
+            worlds.append(w)
+            for c in range(3):
+                W, H = [(24, 16), (17, 33), (40, 24), (1, 1)][int(rng.integers(0, 4))]
+                cam = vt.gen_camera(d, c, W, H)
+                jobs.append((w, cam, ctx.alloc(W * H * 16)))
+        batch = vt.Batch(ctx, jobs, params)
+        for _ in range(2):
+            for _, _, buf in jobs:
+                buf.zero()
+            batch.launch()
+            ctx.sync()
+            for w, cam, buf in jobs:
+                got = buf.download(np.zeros(cam.width * cam.height, vt.HIT_DTYPE))
+                assert np.array_equal(got, vt.render_host(ctx, w, cam, params))
+        batch.close()
+    finally:
+        for _, _, buf in jobs:
+            buf.free()
+        for w in worlds:
+            w.close()

@@ -1,22 +1,26 @@
 // batch.cu -- many scenes x cameras in one graph launch.
 //
 // A batch (jobs of a world, a camera and an output buffer each) is captured
-// once into a CUDA graph and replayed with one cudaGraphLaunch.  Two shapes:
+// once into a CUDA graph and replayed with one cudaGraphLaunch.  Three shapes:
 //
-//   tile (default)  one production k_render launch per job, spread over
-//                   kBatchChains independent chains of the graph, so that the
-//                   tail of one job's launch overlaps the next jobs' work and
-//                   every launch keeps its world and frame in kernel
-//                   parameters (constant bank) as the single-frame path does.
-//   queue           (ctx tuning VT_KERNEL_QUEUE) one persistent launch: every
-//                   job is cut into 16 x 16 pixel units numbered job after
-//                   job; a warp takes one unit at a time from a device
-//                   counter, finds its job by binary search over the jobs'
-//                   first-unit numbers and traces the unit's 256 pixels as
-//                   eight 8 x 4 tiles with the same per-pixel code
-//                   (render_pixel.cuh).  Its per-job state comes from global
-//                   memory, which measured slower than the tile shape once
-//                   the traversal itself got cheaper.
+//   tile (default)  the jobs are cut into chunks of up to kLaunchJobs jobs and
+//                   kLaunchWorlds worlds, and each chunk is ONE launch of
+//                   k_render_jobs whose grid covers every 16 x 16-pixel tile
+//                   of all its jobs.  The chunk's job table (frames, worlds,
+//                   outputs, first tile of each job) is the kernel's
+//                   parameter block itself (__grid_constant__, < 32 KB): a
+//                   block finds its job by a binary search over blockIdx, a
+//                   warp-uniform index, so the world and frame fields come
+//                   from the constant bank as in a single-frame launch.  The
+//                   hardware hands out blocks as SMs free up, so tiles of
+//                   all jobs of a chunk share one launch tail.
+//   per job         (VT_KERNEL_PER_JOB) one production k_render launch per
+//                   job, spread over kBatchChains concurrent chains of the
+//                   graph, so that one job's tail overlaps the next jobs.
+//   queue           (VT_KERNEL_QUEUE) one persistent launch: a warp takes
+//                   16 x 16 pixel units from a device counter, finds its job
+//                   by binary search over the jobs' first-unit numbers and
+//                   reads the job from global memory.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -37,6 +41,75 @@ constexpr int kBatchBlock = 256;
 constexpr int kUnit = 16;  // pixels per unit side
 constexpr int kBatchChains = 8;  // 4, 8, 16 and 32 chains measured within 1% on the 64-scene batch
 
+// ---------------------------------------------------------------- tile shape
+constexpr int kLaunchJobs = 104;
+constexpr int kLaunchWorlds = 32;
+
+// The parameter block of one k_render_jobs launch.  Job j owns the blocks
+// [first_block[j], first_block[j + 1]) of the grid, blocks_x[j] across.
+struct JobChunk {
+    FrameParams frames[kLaunchJobs];
+    WorldView worlds[kLaunchWorlds];
+    uint4* out[kLaunchJobs];
+    unsigned first_block[kLaunchJobs + 1];
+    unsigned blocks_x[kLaunchJobs];
+    unsigned char world_of[kLaunchJobs];
+    int njobs;
+};
+static_assert(sizeof(JobChunk) <= 32764, "a kernel's parameters are limited to 32764 bytes");
+
+// One thread per pixel; the 256-thread block covers a 16 x 16 tile as eight
+// 8 x 4 warp tiles (the single-frame kernel's default shape), with the same
+// register cap (4 blocks per SM).
+template <bool CHECKED>
+__global__ void __launch_bounds__(kBatchBlock, 4) k_render_jobs(const __grid_constant__ JobChunk p, unsigned* status) {
+    const unsigned b = blockIdx.x;
+    int lo = 0, hi = p.njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (p.first_block[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const FrameParams& f = p.frames[lo];
+    const WorldView& w = p.worlds[p.world_of[lo]];
+    const unsigned local = b - p.first_block[lo];
+    const int x0 = (int)(local % p.blocks_x[lo]) * kUnit, y0 = (int)(local / p.blocks_x[lo]) * kUnit;
+    // screen coordinates: the frame's table, else once per block
+    __shared__ float s_col[3][kUnit], s_row[3][kUnit];
+    const bool table = f.screen != nullptr;
+    if (!table) {
+        if (threadIdx.x < kUnit) {
+            s_col[0][threadIdx.x] = ray_u(f, x0 + (int)threadIdx.x);
+            s_col[1][threadIdx.x] = centre_u(f, x0 + (int)threadIdx.x);
+            s_col[2][threadIdx.x] = vignette_u(s_col[1][threadIdx.x]);
+        } else if (threadIdx.x >= 64 && threadIdx.x < 64 + kUnit) {
+            s_row[0][threadIdx.x - 64] = ray_v(f, y0 + (int)threadIdx.x - 64);
+            s_row[1][threadIdx.x - 64] = centre_v(f, y0 + (int)threadIdx.x - 64);
+            s_row[2][threadIdx.x - 64] = vignette_v(s_row[1][threadIdx.x - 64]);
+        }
+        __syncthreads();
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int lx = (warp & 1) * 8 + (lane & 7), ly = (warp >> 1) * 4 + (lane >> 3);
+    const int px = x0 + lx, py = y0 + ly;
+    if (px >= f.width || py >= f.height) return;
+    PixelUV uv;
+    if (table) {
+        uv = table_uv(f, px, py);
+    } else {
+        uv.ru = s_col[0][lx];
+        uv.cu = s_col[1][lx];
+        uv.gu = s_col[2][lx];
+        uv.rv = s_row[0][ly];
+        uv.cv = s_row[1][ly];
+        uv.gv = s_row[2][ly];
+    }
+    PixelCounters pc;
+    p.out[lo][(size_t)py * f.width + px] =
+        render_pixel<false, CHECKED>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, uv, status, pc);
+}
+
+// --------------------------------------------------------------- queue shape
 __global__ void __launch_bounds__(kBatchBlock, 3) k_render_batch(const JobDesc* __restrict__ jobs, int njobs,
                                                                  unsigned total_units, unsigned* __restrict__ counter) {
     const unsigned lane = threadIdx.x & 31u;
@@ -78,7 +151,8 @@ struct vt_batch {
     std::vector<const vt_world*> worlds;
     std::vector<vt_job> jobs;
     vt_params params;
-    vt::JobDesc* d_jobs = nullptr;
+    std::vector<vt::JobChunk> chunks;    // tile shape: one launch each
+    vt::JobDesc* d_jobs = nullptr;       // queue shape
     unsigned* d_counter = nullptr;
     int njobs = 0;
     unsigned total_units = 0;
@@ -90,6 +164,52 @@ struct vt_batch {
 
 using namespace vt;
 
+namespace {
+
+// Cuts the jobs into launch chunks (in job order, each at most kLaunchJobs
+// jobs and kLaunchWorlds distinct worlds); the frames get the context's
+// screen tables (made here if missing: an allocation and a synchronisation).
+vt_status build_chunks(vt_batch* b) {
+    vt_ctx* ctx = b->ctx;
+    b->chunks.clear();
+    JobChunk* c = nullptr;
+    int nworlds = 0;
+    for (size_t i = 0; i < b->jobs.size(); ++i) {
+        const vt_job& j = b->jobs[i];
+        int wi = -1;
+        if (c)
+            for (int k = 0; k < nworlds; ++k)
+                if (c->worlds[k].mask == j.world->d_mask) wi = k;
+        if (!c || c->njobs == kLaunchJobs || (wi < 0 && nworlds == kLaunchWorlds)) {
+            b->chunks.emplace_back();
+            c = &b->chunks.back();
+            std::memset(c, 0, sizeof(*c));
+            nworlds = 0;
+            wi = -1;
+        }
+        if (wi < 0) {
+            wi = nworlds++;
+            c->worlds[wi] = j.world->view();
+        }
+        const int n = c->njobs++;
+        FrameParams f = make_frame(&j.camera, &b->params);
+        vt_status s = screen_table(ctx, f, ctx->stream, true, &f.screen);
+        if (s) return s;
+        c->frames[n] = f;
+        c->out[n] = reinterpret_cast<uint4*>(j.d_out);
+        c->world_of[n] = (unsigned char)wi;
+        c->blocks_x[n] = (unsigned)((j.camera.width + kUnit - 1) / kUnit);
+        const unsigned long long nb =
+            (unsigned long long)c->blocks_x[n] * (unsigned long long)((j.camera.height + kUnit - 1) / kUnit);
+        const unsigned long long end = (unsigned long long)c->first_block[n] + nb;
+        if (end >= (1ull << 31)) return fail(ctx, VT_ERR_ARG, "batch launch too large (blocks >= 2^31)");
+        c->first_block[n + 1] = (unsigned)end;
+    }
+    return VT_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 vt_status vt_batch_create(vt_ctx* ctx, const vt_job* jobs, int32_t n, const vt_params* params, vt_batch** out) {
@@ -100,6 +220,7 @@ vt_status vt_batch_create(vt_ctx* ctx, const vt_job* jobs, int32_t n, const vt_p
     unsigned long long units = 0, pixels = 0;
     vt_batch* b = new (std::nothrow) vt_batch();
     if (!b) return fail(ctx, VT_ERR_OOM, "host allocation failed");
+    b->ctx = ctx;
     for (int i = 0; i < n; ++i) {
         const vt_job& j = jobs[i];
         vt_status s = check_frame_args(ctx, j.world, &j.camera, params);
@@ -125,8 +246,8 @@ vt_status vt_batch_create(vt_ctx* ctx, const vt_job* jobs, int32_t n, const vt_p
         return fail(ctx, VT_ERR_ARG, "batch too large (units >= 2^32)");
     }
     cudaError_t e;
-    if ((e = vt::dev_alloc(&b->d_jobs, host.size() * sizeof(JobDesc))) != cudaSuccess ||
-        (e = vt::dev_alloc(&b->d_counter, sizeof(unsigned))) != cudaSuccess ||
+    if ((e = dev_alloc(&b->d_jobs, host.size() * sizeof(JobDesc))) != cudaSuccess ||
+        (e = dev_alloc(&b->d_counter, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMemcpy(b->d_jobs, host.data(), host.size() * sizeof(JobDesc), cudaMemcpyHostToDevice)) != cudaSuccess) {
         vt_batch_destroy(b);
         return check_cuda(ctx, e, "batch upload");
@@ -136,7 +257,6 @@ vt_status vt_batch_create(vt_ctx* ctx, const vt_job* jobs, int32_t n, const vt_p
         vt_batch_destroy(b);
         return check_cuda(ctx, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     }
-    b->ctx = ctx;
     b->njobs = n;
     b->total_units = (unsigned)units;
     b->pixels = pixels;
@@ -154,13 +274,18 @@ vt_status vt_batch_launch(vt_batch* b, vt_stream stream) {
         vt_status s = update_distances(const_cast<vt_world*>(w), st);
         if (s) return s;
     }
+    const bool checked = (b->params.flags & VT_FLAG_CHECKED) != 0;
     if (!b->exec) {
+        const int shape = ctx->tuning.kernel;
+        if (shape == VT_KERNEL_TILE) {
+            vt_status s = build_chunks(b);   // before the capture: may make screen tables
+            if (s) return s;
+        }
         // capture on private streams: the legacy default stream cannot be captured
         cudaStream_t cap = nullptr;
         cudaStream_t chain[kBatchChains] = {};
         cudaEvent_t fork = nullptr, join[kBatchChains] = {};
         cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
-        const bool queue = ctx->tuning.kernel == VT_KERNEL_QUEUE;
         vt_status s = VT_OK;
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
         for (int k = 0; k < kBatchChains && e == cudaSuccess; ++k) {
@@ -169,17 +294,28 @@ vt_status vt_batch_launch(vt_batch* b, vt_stream stream) {
         }
         if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            if (queue) {
+            if (shape == VT_KERNEL_QUEUE) {
                 cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), cap);
                 k_render_batch<<<b->blocks, kBatchBlock, 0, cap>>>(b->d_jobs, b->njobs, b->total_units, b->d_counter);
             } else {
-                // fork kBatchChains chains off the capture stream, jobs round robin, join
+                // fork chains off the capture stream, launches round robin, join
                 cudaEventRecord(fork, cap);
                 for (int k = 0; k < kBatchChains; ++k) cudaStreamWaitEvent(chain[k], fork, 0);
-                for (size_t j = 0; j < b->jobs.size() && !s; ++j) {
-                    const vt_job& jb = b->jobs[j];
-                    s = launch_render(ctx, jb.world, &jb.camera, &b->params, reinterpret_cast<uint4*>(jb.d_out),
-                                      chain[j % kBatchChains], false);
+                if (shape == VT_KERNEL_TILE) {
+                    for (size_t c = 0; c < b->chunks.size(); ++c) {
+                        const JobChunk& ch = b->chunks[c];
+                        const unsigned blocks = ch.first_block[ch.njobs];
+                        if (checked)
+                            k_render_jobs<true><<<blocks, kBatchBlock, 0, chain[c % kBatchChains]>>>(ch, ctx->d_status);
+                        else
+                            k_render_jobs<false><<<blocks, kBatchBlock, 0, chain[c % kBatchChains]>>>(ch, nullptr);
+                    }
+                } else {
+                    for (size_t j = 0; j < b->jobs.size() && !s; ++j) {
+                        const vt_job& jb = b->jobs[j];
+                        s = launch_render(ctx, jb.world, &jb.camera, &b->params, reinterpret_cast<uint4*>(jb.d_out),
+                                          chain[j % kBatchChains], false);
+                    }
                 }
                 for (int k = 0; k < kBatchChains; ++k) {
                     cudaEventRecord(join[k], chain[k]);
@@ -201,7 +337,7 @@ vt_status vt_batch_launch(vt_batch* b, vt_stream stream) {
     }
     VT_CUDA(ctx, cudaGraphLaunch(b->exec, st));
     // checked jobs may set the status word (their capture noted nothing)
-    if (b->params.flags & VT_FLAG_CHECKED) return note_status_writer(ctx, st);
+    if (checked) return note_status_writer(ctx, st);
     return VT_OK;
 }
 
@@ -210,8 +346,8 @@ vt_status vt_batch_destroy(vt_batch* b) {
     cudaDeviceSynchronize();
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->d_jobs) vt::dev_free(b->d_jobs);
-    if (b->d_counter) vt::dev_free(b->d_counter);
+    vt::dev_free(b->d_jobs);
+    vt::dev_free(b->d_counter);
     delete b;
     return VT_OK;
 }

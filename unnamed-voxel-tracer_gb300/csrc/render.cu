@@ -325,7 +325,7 @@ vt_status check_frame_args(vt_ctx* ctx, const vt_world* world, const vt_camera* 
 // Height in rows of the block tile of the production kernel for a tuning
 // (bands of vt_render_host are multiples of it); 0 for the queue kernel.
 int band_rows_unit(const vt_tuning& tu) {
-    if (tu.kernel != VT_KERNEL_TILE) return 0;
+    if (tu.kernel == VT_KERNEL_QUEUE) return 0;
     if (tu.warp_tile_w == 16) return BlockTile<16>::kH;
     if (tu.warp_tile_w == 32) return BlockTile<32>::kH;
     return BlockTile<8>::kH;
@@ -536,7 +536,7 @@ vt_status vt_render_host(vt_ctx* ctx, const vt_world* world, const vt_camera* ca
     uint4* d_out = reinterpret_cast<uint4*>(d_scratch);
     const int rows_tile = band_rows_unit(ctx->tuning);
     // (bounce rays go through the deferred pass, one launch for the frame)
-    const bool pipelined = ctx->tuning.kernel == VT_KERNEL_TILE && W * H >= kPipelinePixels &&
+    const bool pipelined = ctx->tuning.kernel != VT_KERNEL_QUEUE && W * H >= kPipelinePixels &&
                            (params->flags & VT_FLAG_CHECKED) == 0 && (params->rays & VT_RAYS_BOUNCE) == 0 &&
                            rows_tile > 0;
     if (!pipelined) {

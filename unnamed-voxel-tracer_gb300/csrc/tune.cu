@@ -18,7 +18,7 @@
 namespace {
 
 bool valid(const vt_tuning& t) {
-    if (t.kernel == VT_KERNEL_TILE)
+    if (t.kernel == VT_KERNEL_TILE || t.kernel == VT_KERNEL_PER_JOB)
         return (t.warp_tile_w == 8 || t.warp_tile_w == 16 || t.warp_tile_w == 32) && (t.occupancy == 0 || t.occupancy == 1);
     if (t.kernel == VT_KERNEL_QUEUE) return t.batch >= 1 && t.batch <= 32;
     return false;

@@ -226,6 +226,10 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
                         cudaStream_t stream, bool stats, int row0 = 0, int row1 = -1, bool allow_defer = false,
                         bool new_table = true);
 struct FrameParams;
+// The context's screen table for a frame's image size and field of view
+// (made on first use when `create` and the stream is not being captured;
+// *out stays null when none can be had).
+vt_status screen_table(vt_ctx* ctx, const FrameParams& f, cudaStream_t st, bool create, const float4** out);
 // The deferred bounce pass: queue buffers for `pixels` rays, and the trace +
 // shade kernels for a frame whose render kernel queued them.
 vt_status bounce_buffers(vt_ctx* ctx, size_t pixels);

@@ -34,7 +34,7 @@ STATUS_NAMES = {0: "VT_OK", 1: "VT_ERR_ARG", 2: "VT_ERR_OOM", 3: "VT_ERR_CUDA", 
 RAYS_PRIMARY, RAYS_SHADOW, RAYS_BOUNCE = 1, 2, 4
 SHADE_NONE, SHADE_REFERENCE, SHADE_LAMBERT = 0, 1, 2
 FLAG_CROSSHAIR, FLAG_VIGNETTE, FLAG_CHECKED = 1, 2, 4
-KERNEL_TILE, KERNEL_QUEUE = 0, 1
+KERNEL_TILE, KERNEL_QUEUE, KERNEL_PER_JOB = 0, 1, 2
 HIT_PRIMARY, HIT_SHADOWED, HIT_BOUNCE, HIT_ENTITY = 1, 2, 4, 8
 
 
