@@ -402,7 +402,7 @@ def launch_floor(torch, n: int) -> dict:
 def measure_config3(vt, scenes, ctx, torch, peak, peak_kind, oracle_py) -> dict:
     """64 cube scenes (edge log-uniform in [32, 512]) x 1-8 cameras: one
     CUDA-graph launch of the batch vs one vt_render launch per camera.  The
-    default batch graph holds one launch per chunk of up to 104 jobs; the
+    default batch graph holds one launch per world (all its cameras); the
     per-job shape (one launch per camera on 8 concurrent chains) and the
     queue shape (one persistent kernel over 16x16 units) are timed too."""
     sc, params = scenes.config3()

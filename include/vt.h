@@ -358,9 +358,9 @@ vt_status vt_brickmap_edit(vt_ctx* ctx, vt_brickmap* bm, const vt_camera* cam, i
 /* ----------------------------------------------------------------- batch
  * Many scenes x cameras in one graph launch (no counterpart in the reference,
  * which renders one camera per frame, game.zig:232-256).  Under the default
- * tuning (VT_KERNEL_TILE) the graph holds one render launch per chunk of up
- * to 104 jobs and 32 worlds, whose grid covers the 16x16-pixel tiles of all
- * its jobs (the chunk's job table travels as the launch's parameters); under
+ * tuning (VT_KERNEL_TILE) the graph holds one render launch per world (its
+ * consecutive jobs, up to 256), whose grid covers the 16x16-pixel tiles of
+ * all those jobs (the job table travels as the launch's parameters); under
  * VT_KERNEL_PER_JOB it holds one render launch per job on eight concurrent
  * chains; under VT_KERNEL_QUEUE one persistent kernel that pulls 16x16-pixel
  * units of all jobs from a device work queue.  Every job's records are

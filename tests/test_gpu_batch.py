@@ -85,9 +85,10 @@ def test_batch_captured_in_a_fresh_context(vt):
 
 @pytest.mark.parametrize("checked", [False, True], ids=["plain", "checked"])
 def test_batch_many_chunks(vt, ctx, checked):
-    """More jobs (126) and worlds (42) than one chunked launch holds (104 and
-    32): the batch spans several launches; small and ragged frames; the
-    bounds-checked variant too.  Every job equals its own vt_render."""
+    """126 jobs over 42 worlds (one launch per world in the default shape),
+    small and ragged frames, the bounds-checked variant too, and one world
+    with more jobs (300 one-pixel cameras) than one launch holds (256).  Every
+    job equals its own vt_render."""
     rng = np.random.default_rng(41)
     flags = vt.FLAG_CROSSHAIR | vt.FLAG_VIGNETTE | (vt.FLAG_CHECKED if checked else 0)
     params = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=vt.gen_sun(41), flags=flags)
@@ -103,6 +104,9 @@ def test_batch_many_chunks(vt, ctx, checked):
                 W, H = [(24, 16), (17, 33), (40, 24), (1, 1)][int(rng.integers(0, 4))]
                 cam = vt.gen_camera(d, c, W, H)
                 jobs.append((w, cam, ctx.alloc(W * H * 16)))
+        for c in range(300):
+            cam = vt.gen_camera(d, 1000 + c, 1 + c % 3, 1 + c % 2)
+            jobs.append((w, cam, ctx.alloc(cam.width * cam.height * 16)))
         batch = vt.Batch(ctx, jobs, params)
         for _ in range(2):
             for _, _, buf in jobs:

@@ -3,17 +3,18 @@
 // A batch (jobs of a world, a camera and an output buffer each) is captured
 // once into a CUDA graph and replayed with one cudaGraphLaunch.  Three shapes:
 //
-//   tile (default)  the jobs are cut into chunks of up to kLaunchJobs jobs and
-//                   kLaunchWorlds worlds, and each chunk is ONE launch of
-//                   k_render_jobs whose grid covers every 16 x 16-pixel tile
-//                   of all its jobs.  The chunk's job table (frames, worlds,
-//                   outputs, first tile of each job) is the kernel's
-//                   parameter block itself (__grid_constant__, < 32 KB): a
-//                   block finds its job by a binary search over blockIdx, a
-//                   warp-uniform index, so the world and frame fields come
-//                   from the constant bank as in a single-frame launch.  The
-//                   hardware hands out blocks as SMs free up, so tiles of
-//                   all jobs of a chunk share one launch tail.
+//   tile (default)  the consecutive jobs of each world (up to kLaunchJobs)
+//                   are ONE launch of k_render_jobs whose grid covers every
+//                   16 x 16-pixel tile of all of them, on kBatchChains
+//                   concurrent chains of the graph.  The launch's job table
+//                   (the world, the shared frame settings, each job's camera,
+//                   output and first tile) is the kernel's parameter block
+//                   itself (__grid_constant__, < 32 KB): a block finds its
+//                   job by a binary search over blockIdx, and the world's
+//                   fields are constant-bank operands as in a single-frame
+//                   launch.  The hardware hands out blocks as SMs free up, so
+//                   the tiles of all cameras of a world share one launch
+//                   tail.
 //   per job         (VT_KERNEL_PER_JOB) one production k_render launch per
 //                   job, spread over kBatchChains concurrent chains of the
 //                   graph, so that one job's tail overlaps the next jobs.
@@ -42,19 +43,30 @@ constexpr int kUnit = 16;  // pixels per unit side
 constexpr int kBatchChains = 8;  // 4, 8, 16 and 32 chains measured within 1% on the 64-scene batch
 
 // ---------------------------------------------------------------- tile shape
-constexpr int kLaunchJobs = 104;
-constexpr int kLaunchWorlds = 32;
+constexpr int kLaunchJobs = 256;
 
-// The parameter block of one k_render_jobs launch.  Job j owns the blocks
-// [first_block[j], first_block[j + 1]) of the grid, blocks_x[j] across.
+// Per-job camera fields of a tile-shape launch.
+struct JobCam {
+    float pos[3];
+    float view[16];
+    float tan_half_fov;
+    int width, height;
+    const float4* screen;
+    uint4* out;
+    unsigned blocks_x;
+};
+
+// The parameter block of one k_render_jobs launch: jobs of ONE world.  The
+// world and the frame settings the jobs share sit at fixed offsets (read as
+// constant-bank operands, as in a single-frame launch: a dynamically indexed
+// world measured 12% slower per pixel); only the cameras are indexed.  Job j
+// owns the blocks [first_block[j], first_block[j + 1]) of the grid.
 struct JobChunk {
-    FrameParams frames[kLaunchJobs];
-    WorldView worlds[kLaunchWorlds];
-    uint4* out[kLaunchJobs];
-    unsigned first_block[kLaunchJobs + 1];
-    unsigned blocks_x[kLaunchJobs];
-    unsigned char world_of[kLaunchJobs];
+    WorldView w;
+    FrameParams f;  // shared settings; the camera fields are the job's
     int njobs;
+    unsigned first_block[kLaunchJobs + 1];
+    JobCam cam[kLaunchJobs];
 };
 static_assert(sizeof(JobChunk) <= 32764, "a kernel's parameters are limited to 32764 bytes");
 
@@ -70,10 +82,19 @@ __global__ void __launch_bounds__(kBatchBlock, 4) k_render_jobs(const __grid_con
         if (p.first_block[mid] <= b) lo = mid;
         else hi = mid - 1;
     }
-    const FrameParams& f = p.frames[lo];
-    const WorldView& w = p.worlds[p.world_of[lo]];
+    const JobCam& jc = p.cam[lo];
+    FrameParams f = p.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) f.pos[k] = jc.pos[k];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) f.view[k] = jc.view[k];
+    f.tan_half_fov = jc.tan_half_fov;
+    f.width = jc.width;
+    f.height = jc.height;
+    f.row_end = jc.height;
+    f.screen = jc.screen;
     const unsigned local = b - p.first_block[lo];
-    const int x0 = (int)(local % p.blocks_x[lo]) * kUnit, y0 = (int)(local / p.blocks_x[lo]) * kUnit;
+    const int x0 = (int)(local % jc.blocks_x) * kUnit, y0 = (int)(local / jc.blocks_x) * kUnit;
     // screen coordinates: the frame's table, else once per block
     __shared__ float s_col[3][kUnit], s_row[3][kUnit];
     const bool table = f.screen != nullptr;
@@ -105,8 +126,8 @@ __global__ void __launch_bounds__(kBatchBlock, 4) k_render_jobs(const __grid_con
         uv.gv = s_row[2][ly];
     }
     PixelCounters pc;
-    p.out[lo][(size_t)py * f.width + px] =
-        render_pixel<false, CHECKED>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, uv, status, pc);
+    const uint4 rec = render_pixel<false, CHECKED>(p.w, CoarseGlobal{p.w.coarse}, p.w.cdist, f, px, py, uv, status, pc);
+    p.cam[lo].out[(size_t)py * f.width + px] = rec;
 }
 
 // --------------------------------------------------------------- queue shape
@@ -166,41 +187,37 @@ using namespace vt;
 
 namespace {
 
-// Cuts the jobs into launch chunks (in job order, each at most kLaunchJobs
-// jobs and kLaunchWorlds distinct worlds); the frames get the context's
-// screen tables (made here if missing: an allocation and a synchronisation).
+// Cuts the jobs into launch chunks: consecutive jobs of one world, at most
+// kLaunchJobs each.  The frames get the context's screen tables (made here if
+// missing: an allocation and a synchronisation).
 vt_status build_chunks(vt_batch* b) {
     vt_ctx* ctx = b->ctx;
     b->chunks.clear();
     JobChunk* c = nullptr;
-    int nworlds = 0;
     for (size_t i = 0; i < b->jobs.size(); ++i) {
         const vt_job& j = b->jobs[i];
-        int wi = -1;
-        if (c)
-            for (int k = 0; k < nworlds; ++k)
-                if (c->worlds[k].mask == j.world->d_mask) wi = k;
-        if (!c || c->njobs == kLaunchJobs || (wi < 0 && nworlds == kLaunchWorlds)) {
-            b->chunks.emplace_back();
-            c = &b->chunks.back();
-            std::memset(c, 0, sizeof(*c));
-            nworlds = 0;
-            wi = -1;
-        }
-        if (wi < 0) {
-            wi = nworlds++;
-            c->worlds[wi] = j.world->view();
-        }
-        const int n = c->njobs++;
         FrameParams f = make_frame(&j.camera, &b->params);
         vt_status s = screen_table(ctx, f, ctx->stream, true, &f.screen);
         if (s) return s;
-        c->frames[n] = f;
-        c->out[n] = reinterpret_cast<uint4*>(j.d_out);
-        c->world_of[n] = (unsigned char)wi;
-        c->blocks_x[n] = (unsigned)((j.camera.width + kUnit - 1) / kUnit);
+        if (!c || c->njobs == kLaunchJobs || c->w.mask != j.world->d_mask) {
+            b->chunks.emplace_back();
+            c = &b->chunks.back();
+            std::memset(c, 0, sizeof(*c));
+            c->w = j.world->view();
+            c->f = f;
+        }
+        const int n = c->njobs++;
+        JobCam& jc = c->cam[n];
+        for (int k = 0; k < 3; ++k) jc.pos[k] = f.pos[k];
+        for (int k = 0; k < 16; ++k) jc.view[k] = f.view[k];
+        jc.tan_half_fov = f.tan_half_fov;
+        jc.width = f.width;
+        jc.height = f.height;
+        jc.screen = f.screen;
+        jc.out = reinterpret_cast<uint4*>(j.d_out);
+        jc.blocks_x = (unsigned)((j.camera.width + kUnit - 1) / kUnit);
         const unsigned long long nb =
-            (unsigned long long)c->blocks_x[n] * (unsigned long long)((j.camera.height + kUnit - 1) / kUnit);
+            (unsigned long long)jc.blocks_x * (unsigned long long)((j.camera.height + kUnit - 1) / kUnit);
         const unsigned long long end = (unsigned long long)c->first_block[n] + nb;
         if (end >= (1ull << 31)) return fail(ctx, VT_ERR_ARG, "batch launch too large (blocks >= 2^31)");
         c->first_block[n + 1] = (unsigned)end;
