@@ -437,10 +437,17 @@ vt_status vt_shade_backward_views(vt_ctx* ctx, const vt_world* world, int32_t n,
 #define VT_KERNEL_QUEUE   1 /* persistent warps refilling lanes from a pixel queue */
 #define VT_KERNEL_PER_JOB 2 /* as VT_KERNEL_TILE for single frames; a batch: one launch per job */
 typedef struct {
-    int32_t kernel;       /* VT_KERNEL_* */
-    int32_t warp_tile_w;  /* VT_KERNEL_TILE: a warp's tile is w x (32/w) pixels, w in {8, 16, 32} */
-    int32_t occupancy;    /* VT_KERNEL_TILE: 1 = register budget capped for 4 blocks (32 warps) per SM */
-    int32_t batch;        /* VT_KERNEL_QUEUE: parked lanes (1..32) that trigger a refill pass */
+    int32_t kernel;        /* VT_KERNEL_* */
+    int32_t warp_tile_w;   /* VT_KERNEL_TILE: a warp's tile is w x (32/w) pixels, w in {4, 8, 16, 32} */
+    int32_t occupancy;     /* VT_KERNEL_TILE: 1 = register budget capped for 4 blocks (32 warps) per SM */
+    int32_t batch;         /* VT_KERNEL_QUEUE: parked lanes (1..32) that trigger a refill pass */
+    int32_t share_bricks;  /* VT_KERNEL_TILE with w = 8 and the cap: 1 = lanes of a warp that look up the
+                              same brick word share one load (__match_any_sync + __shfl_sync) */
+    int32_t l2_persist;    /* 1 = render launches carry an L2 access-policy window over the world's brick
+                              words (persisting, as much as the device's persisting L2 holds) */
+    int32_t bounce_refill; /* deferred bounce rays: idle lanes (1..32) that make a warp refill; 0 = 8 */
+    int32_t bounce_walk;   /* deferred bounce rays: 0 = brick-run walk (unit steps of an occupied brick
+                              in an inner loop), 1 = one advance per turn for jumps and unit steps alike */
 } vt_tuning;
 vt_status vt_set_tuning(vt_ctx* ctx, const vt_tuning* tuning);
 vt_status vt_get_tuning(vt_ctx* ctx, vt_tuning* tuning);

@@ -312,17 +312,20 @@ extern "C" int ht_trace_rays(const int32_t dims[3], const uint8_t* dense, const 
         vt::TraceCounters cnt;
         bool hit;
         if (fast) {
-            // the production walk, one step at a time; counters[0] = steps taken
+            // the production walk (fast 1: step, fast 2: step_flat), one step
+            // at a time; counters[0] = steps taken
             vt::Walker wk;
             hit = false;
             if (wk.start(w, r.o, r.d, max_steps)) {
                 int s;
                 const bool near = vt::near_origin(r.o);
                 do {
-                    s = near ? wk.step<true, true, true>(w, w.cdist, h) : wk.step<true, true, false>(w, w.cdist, h);
+                    if (fast == 2) s = near ? wk.step_flat<true>(w, w.cdist, h) : wk.step_flat<false>(w, w.cdist, h);
+                    else s = near ? wk.step<true, true, true>(w, w.cdist, h) : wk.step<true, true, false>(w, w.cdist, h);
                     counters[0]++;
                 } while (s == vt::Walker::kMore);
                 hit = s == vt::Walker::kHit;
+                if (hit && fast == 2) h.mat = w.mats[(size_t)wk.wi * 64u + wk.vb];   // step_flat reads no material
             }
         } else {
             hit = vt::trace_p<true, true, true>(w, vt::CoarseGlobal{w.coarse}, r, max_steps, h, cnt, &status);

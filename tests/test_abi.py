@@ -35,15 +35,15 @@ def test_struct_layouts_match_c(vtlib, tmp_path):
     prog = tmp_path / "sizes.c"
     prog.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "vt.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(vt_camera), sizeof(vt_params),"
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(vt_camera), sizeof(vt_params),"
         " sizeof(vt_hit), sizeof(vt_stats), sizeof(vt_gen_desc), sizeof(vt_world_info), sizeof(vt_world_desc),"
-        " offsetof(vt_gen_desc, seed));return 0;}\n")
+        " offsetof(vt_gen_desc, seed), sizeof(vt_tuning));return 0;}\n")
     exe = tmp_path / "sizes"
     subprocess.run(["gcc", "-std=c99", "-I", str(ROOT / "include"), str(prog), "-o", str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     want = [C.sizeof(vtlib.Camera_t), C.sizeof(vtlib.Params_t), vtlib.HIT_DTYPE.itemsize, C.sizeof(vtlib.Stats_t),
             C.sizeof(vtlib.GenDesc_t), C.sizeof(vtlib.WorldInfo_t), C.sizeof(vtlib.WorldDesc_t),
-            vtlib.GenDesc_t.seed.offset]
+            vtlib.GenDesc_t.seed.offset, C.sizeof(vtlib.Tuning_t)]
     assert got == want
 
 

@@ -130,8 +130,10 @@ def test_config0_frame(vt, oracle, ctx, shade):
     assert (gpu["flags"] & vt.HIT_PRIMARY).mean() > 0.3
 
 
-TUNINGS = [dict(kernel=0, warp_tile_w=tw, occupancy=o) for tw in (8, 16, 32) for o in (0, 1)] + \
-          [dict(kernel=1, batch=b) for b in (1, 16, 32)]
+TUNINGS = [dict(kernel=0, warp_tile_w=tw, occupancy=o) for tw in (4, 8, 16, 32) for o in (0, 1)] + \
+          [dict(kernel=0, warp_tile_w=8, occupancy=1, share_bricks=1), dict(kernel=0, l2_persist=1),
+           dict(kernel=2, warp_tile_w=16, occupancy=1)] + \
+          [dict(kernel=1, batch=b) for b in (1, 16, 32)] + [dict(kernel=1, batch=16, l2_persist=1)]
 
 
 @pytest.fixture
@@ -229,6 +231,25 @@ def test_bounce_rays(vt, oracle, ctx):
     gpu, ref, _ = render_both(vt, oracle, ctx, mats, cam, p)
     compare(gpu, ref)
     assert (gpu["flags"] & vt.HIT_BOUNCE).any()
+
+
+BOUNCE_TUNINGS = [dict(bounce_walk=wk, bounce_refill=r) for wk in (0, 1) for r in (0, 1, 4, 16, 32)] + \
+                 [dict(bounce_walk=1, l2_persist=1), dict(warp_tile_w=4, bounce_walk=1, bounce_refill=8)]
+
+
+@pytest.mark.parametrize("tuning", BOUNCE_TUNINGS, ids=lambda t: "-".join(f"{k}{v}" for k, v in t.items()))
+def test_bounce_pass_variants(vt, oracle, tuned, tuning):
+    """The deferred bounce pass under every walk and refill setting the
+    autotuner may pick (and with the L2 window): the records equal the
+    oracle's."""
+    d = vt.gen_desc((256, 128, 256), seed=12, trees=60, caves=True)
+    mats = vt.gen_world(d)
+    cam = vt.gen_camera(d, 2, 300, 170)
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW | vt.RAYS_BOUNCE, seed=77, sun_dir=vt.gen_sun(12))
+    tuned.set_tuning(**tuning)
+    gpu, ref, _ = render_both(vt, oracle, tuned, mats, cam, p)
+    compare(gpu, ref)
+    assert (gpu["flags"] & vt.HIT_BOUNCE).any() and ((gpu["flags"] & 5) == 1).any()
 
 
 def test_lambert_and_checked_variant(vt, oracle, ctx):

@@ -66,7 +66,7 @@ def random_rays(rng, dims, n):
 
 def check(ht, oracle, mats, o, d, steps):
     ref = oracle.trace_rays(oracle.OracleWorld(mats), o, d, steps)
-    for fast in (0, 1):
+    for fast in (0, 1, 2):   # model walk, production walk, its one-path variant (bounce pass)
         got, _ = run_host(ht, mats, o, d, steps, fast)
         compare_exact(got, ref, o, d, fields=("voxel", "face", "material", "flags"))
 

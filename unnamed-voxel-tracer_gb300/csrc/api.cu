@@ -81,6 +81,40 @@ cudaError_t host_free(void* p) {
     return e;
 }
 
+vt_status l2_window(vt_ctx* ctx, const vt_world* world, cudaStream_t st, L2Window* guard) {
+    if (!ctx->tuning.l2_persist || !st) return VT_OK;   // (the legacy default stream takes no attributes)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return VT_OK;
+    }
+    if (!ctx->l2_setaside) {
+        // the persisting set-aside of this process's context (undone when the
+        // context goes; nothing outlasts the process)
+        int maxp = 0, maxw = 0;
+        VT_CUDA(ctx, cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, ctx->device));
+        VT_CUDA(ctx, cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device));
+        ctx->l2_persist_max = (size_t)(maxp > 0 ? maxp : 0);
+        ctx->l2_window_max = (size_t)(maxw > 0 ? maxw : 0);
+        if (ctx->l2_persist_max) VT_CUDA(ctx, cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, ctx->l2_persist_max));
+        ctx->l2_setaside = true;
+    }
+    if (!ctx->l2_persist_max || !ctx->l2_window_max) return VT_OK;
+    VT_CUDA(ctx, cudaStreamGetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &guard->prev));
+    const size_t words = world->nchunks * (size_t)kBricksPerChunk * 8u;
+    const size_t bytes = words < ctx->l2_window_max ? words : ctx->l2_window_max;
+    cudaStreamAttrValue v = {};
+    v.accessPolicyWindow.base_ptr = world->d_mask;
+    v.accessPolicyWindow.num_bytes = bytes;
+    v.accessPolicyWindow.hitRatio = bytes <= ctx->l2_persist_max ? 1.0f : (float)ctx->l2_persist_max / (float)bytes;
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    VT_CUDA(ctx, cudaStreamSetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &v));
+    guard->st = st;
+    guard->set = true;
+    return VT_OK;
+}
+
 vt_status take_status(vt_ctx* ctx, unsigned st) {
     if (!st) return VT_OK;
     VT_CUDA(ctx, cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
@@ -185,6 +219,11 @@ vt_status vt_ctx_destroy(vt_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->l2_setaside) {
+        cudaDeviceSynchronize();
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    }
     for (int i = 0; i < kBandStreams; ++i)
         if (ctx->band_stream[i]) {
             cudaStreamSynchronize(ctx->band_stream[i]);

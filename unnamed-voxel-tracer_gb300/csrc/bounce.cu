@@ -10,7 +10,8 @@ namespace {
 
 constexpr int kBounceBlock = 256;
 // a warp takes new rays from the queue once this many of its lanes are idle
-// (1, 4, 8, 16, 24 measured on a 4K cave-world frame: 8 is fastest)
+// (tuning bounce_refill; 1, 4, 8, 16, 24 measured on a 4K cave-world frame
+// with the brick-run walk: 8 is fastest)
 constexpr int kRefill = 8;
 // walk iterations a busy lane makes between two refill checks (1, 2, 3, 4, 8
 // measured on the same frame: 2 and 3 are fastest, 4% less bounce time than 1)
@@ -19,10 +20,13 @@ constexpr int kActions = 2;
 // Persistent: every warp loops until the queue is drained.  A lane walks one
 // ray at a time, kActions iterations of the walk per loop turn; open[j] receives 1
 // when ray j leaves without a hit (the sky lights its pixel), 0 otherwise.
+// FLAT: walk with Walker::step_flat (one code path for jumps and unit steps)
+// instead of Walker::step.
+template <bool FLAT>
 __global__ void __launch_bounds__(kBounceBlock) k_bounce_trace(WorldView w, const BounceJob* __restrict__ jobs,
                                                                const unsigned* __restrict__ counters,
                                                                unsigned* __restrict__ next, unsigned char* open,
-                                                               int max_steps) {
+                                                               int max_steps, int refill) {
     const unsigned total = counters[0];
     const unsigned lane = threadIdx.x & 31u;
     const unsigned below = (1u << lane) - 1u;
@@ -31,7 +35,7 @@ __global__ void __launch_bounds__(kBounceBlock) k_bounce_trace(WorldView w, cons
     unsigned job = 0;
     for (;;) {
         const unsigned idle = __ballot_sync(0xFFFFFFFFu, !busy);
-        if (idle == 0xFFFFFFFFu || __popc(idle) >= kRefill) {
+        if (idle == 0xFFFFFFFFu || __popc(idle) >= refill) {
             unsigned base = 0;
             if (lane == 0) base = atomicAdd(next, (unsigned)__popc(idle));
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
@@ -48,7 +52,8 @@ __global__ void __launch_bounds__(kBounceBlock) k_bounce_trace(WorldView w, cons
         if (busy) {
             TraceHit h;
             int s = Walker::kMore;
-            for (int a = 0; a < kActions && s == Walker::kMore; ++a) s = wk.step<false, true, true>(w, w.cdist, h);
+            for (int a = 0; a < kActions && s == Walker::kMore; ++a)
+                s = FLAT ? wk.step_flat<true>(w, w.cdist, h) : wk.step<false, true, true>(w, w.cdist, h);
             if (s != Walker::kMore) {
                 open[job] = s == Walker::kHit ? 0 : 1;
                 busy = false;
@@ -105,14 +110,21 @@ vt_status bounce_buffers(vt_ctx* ctx, size_t pixels) {
 
 vt_status launch_bounce(vt_ctx* ctx, const vt_world* world, const FrameParams& f, uint4* d_out, cudaStream_t st) {
     const WorldView w = world->view();
-    if (ctx->bounce_blocks == 0) {
+    const int flat = ctx->tuning.bounce_walk == 1 ? 1 : 0;
+    const int refill = ctx->tuning.bounce_refill > 0 ? ctx->tuning.bounce_refill : kRefill;
+    if (ctx->bounce_blocks[flat] == 0) {
         int nb = 0;
-        VT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bounce_trace, kBounceBlock, 0));
-        ctx->bounce_blocks = ctx->sm_count * (nb > 0 ? nb : 1);
+        if (flat) VT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bounce_trace<true>, kBounceBlock, 0));
+        else VT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bounce_trace<false>, kBounceBlock, 0));
+        ctx->bounce_blocks[flat] = ctx->sm_count * (nb > 0 ? nb : 1);
     }
     const BounceJob* jobs = reinterpret_cast<const BounceJob*>(ctx->d_bounce_jobs);
-    k_bounce_trace<<<ctx->bounce_blocks, kBounceBlock, 0, st>>>(w, jobs, ctx->d_bounce_ctr, ctx->d_bounce_ctr + 1,
-                                                                ctx->d_bounce_open, f.bounce_max_steps);
+    if (flat)
+        k_bounce_trace<true><<<ctx->bounce_blocks[1], kBounceBlock, 0, st>>>(
+            w, jobs, ctx->d_bounce_ctr, ctx->d_bounce_ctr + 1, ctx->d_bounce_open, f.bounce_max_steps, refill);
+    else
+        k_bounce_trace<false><<<ctx->bounce_blocks[0], kBounceBlock, 0, st>>>(
+            w, jobs, ctx->d_bounce_ctr, ctx->d_bounce_ctr + 1, ctx->d_bounce_open, f.bounce_max_steps, refill);
     VT_CUDA(ctx, cudaGetLastError());
     k_bounce_finish<<<ctx->sm_count * 8, kBounceBlock, 0, st>>>(w, f, jobs, ctx->d_bounce_ctr, ctx->d_bounce_open,
                                                                 d_out);

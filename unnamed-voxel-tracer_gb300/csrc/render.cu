@@ -43,7 +43,9 @@ struct BlockTile {
     static_assert(kW <= 64 && kH <= kBlock - 64, "the column and row tables are filled by distinct threads");
 };
 
-template <bool STATS, bool CHECKED, bool SMEM, int TW, bool OCC>
+// SHARE: the lanes of a warp that look up the same brick word share one load
+// (Walker::brick_word).
+template <bool STATS, bool CHECKED, bool SMEM, int TW, bool OCC, bool SHARE = false>
 __global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldView w, FrameParams f, uint4* __restrict__ out,
                                                                unsigned* status, unsigned long long* counters) {
     // shared copy of the coarse bits for the model traversal (STATS or
@@ -89,7 +91,8 @@ __global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldVi
         }
         uint4 rec;
         if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, w.cdist, f, px, py, uv, status, pc);
-        else rec = render_pixel<STATS, CHECKED>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, uv, status, pc);
+        else rec = render_pixel<STATS, CHECKED, CoarseGlobal, SHARE>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, uv,
+                                                                     status, pc);
         out[(size_t)py * f.width + px] = rec;
     }
     flush_counters<STATS>(pc, counters);
@@ -326,6 +329,7 @@ vt_status check_frame_args(vt_ctx* ctx, const vt_world* world, const vt_camera* 
 // (bands of vt_render_host are multiples of it); 0 for the queue kernel.
 int band_rows_unit(const vt_tuning& tu) {
     if (tu.kernel == VT_KERNEL_QUEUE) return 0;
+    if (tu.warp_tile_w == 4) return BlockTile<4>::kH;
     if (tu.warp_tile_w == 16) return BlockTile<16>::kH;
     if (tu.warp_tile_w == 32) return BlockTile<32>::kH;
     return BlockTile<8>::kH;
@@ -412,6 +416,11 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
     }
     const size_t sm = use_smem ? smem : 0;
     const vt_tuning& tu = ctx->tuning;
+    L2Window l2;  // restores the stream's access-policy window when the launches are queued
+    {
+        vt_status s = l2_window(ctx, world, stream, &l2);
+        if (s) return s;
+    }
     if (!stats && !checked && tu.kernel == VT_KERNEL_QUEUE) {
         // persistent kernel over a pixel queue; the queue counter is one slot
         // of the context's ring, zeroed on this stream before the launch
@@ -446,10 +455,11 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         f.bounce_jobs = ctx->d_bounce_jobs;
         f.bounce_count = ctx->d_bounce_ctr;
     }
-#define VT_LAUNCH(S, C, M, TW, O)                                                                               \
-    k_render<S, C, M, TW, O><<<dim3((cam->width + BlockTile<TW>::kW - 1) / BlockTile<TW>::kW,                   \
-                                    (rows + BlockTile<TW>::kH - 1) / BlockTile<TW>::kH),                        \
-                               kBlock, sm, stream>>>(w, f, d_out, ctx->d_status, ctx->d_counters)
+#define VT_LAUNCH_X(S, C, M, TW, O, SH)                                                                         \
+    k_render<S, C, M, TW, O, SH><<<dim3((cam->width + BlockTile<TW>::kW - 1) / BlockTile<TW>::kW,               \
+                                        (rows + BlockTile<TW>::kH - 1) / BlockTile<TW>::kH),                    \
+                                   kBlock, sm, stream>>>(w, f, d_out, ctx->d_status, ctx->d_counters)
+#define VT_LAUNCH(S, C, M, TW, O) VT_LAUNCH_X(S, C, M, TW, O, false)
 #define VT_LAUNCH_M(S, C, TW, O)      \
     if (use_smem) VT_LAUNCH(S, C, true, TW, O); \
     else VT_LAUNCH(S, C, false, TW, O)
@@ -457,6 +467,9 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         VT_LAUNCH_M(true, true, 8, false);
     } else if (checked) {
         VT_LAUNCH_M(false, true, 8, false);
+    } else if (tu.warp_tile_w == 4) {
+        if (tu.occupancy) { VT_LAUNCH(false, false, false, 4, true); }
+        else { VT_LAUNCH(false, false, false, 4, false); }
     } else if (tu.warp_tile_w == 16) {
         if (tu.occupancy) { VT_LAUNCH(false, false, false, 16, true); }
         else { VT_LAUNCH(false, false, false, 16, false); }
@@ -464,11 +477,13 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         if (tu.occupancy) { VT_LAUNCH(false, false, false, 32, true); }
         else { VT_LAUNCH(false, false, false, 32, false); }
     } else {
-        if (tu.occupancy) { VT_LAUNCH(false, false, false, 8, true); }
+        if (tu.occupancy && tu.share_bricks) { VT_LAUNCH_X(false, false, false, 8, true, true); }
+        else if (tu.occupancy) { VT_LAUNCH(false, false, false, 8, true); }
         else { VT_LAUNCH(false, false, false, 8, false); }
     }
 #undef VT_LAUNCH_M
 #undef VT_LAUNCH
+#undef VT_LAUNCH_X
     VT_CUDA(ctx, cudaGetLastError());
     if (stats || checked) return note_status_writer(ctx, stream);  // the model walk checks its indexes
     if (defer) return launch_bounce(ctx, world, f, d_out, stream);

@@ -18,18 +18,19 @@ struct PixelCounters {
 // runs trace_fast.  Both give identical results.
 // NEAR: the caller knows the origin passes near_origin (secondary rays start
 // on a hit inside the grid); otherwise the primary ray checks it once.
-template <bool STATS, bool CHECKED, bool MAT, bool NEAR, class Coarse>
+// SHARE: brick words shared between the lanes of a warp (Walker::brick_word).
+template <bool STATS, bool CHECKED, bool MAT, bool NEAR, bool SHARE, class Coarse>
 __device__ __forceinline__ bool trace_any(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
                                           const PRay& r, int max_steps, TraceHit& h, TraceCounters& cnt,
                                           unsigned* status) {
     if (STATS || CHECKED) return trace_p<STATS, CHECKED, MAT>(w, coarse, r, max_steps, h, cnt, status);
-    if (NEAR || near_origin(r.o)) return trace_fast<MAT, true, true>(w, cd, r, max_steps, h);
-    return trace_fast<MAT, true, false>(w, cd, r, max_steps, h);
+    if (NEAR || near_origin(r.o)) return trace_fast<MAT, true, true, SHARE>(w, cd, r, max_steps, h);
+    return trace_fast<MAT, true, false, SHARE>(w, cd, r, max_steps, h);
 }
 
 // uv: the pixel's screen coordinates (pixel_uv(f, px, py); the frame kernel
 // reads them from the frame's screen table or its per-block tables).
-template <bool STATS, bool CHECKED, class Coarse>
+template <bool STATS, bool CHECKED, class Coarse, bool SHARE = false>
 __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
                                               const FrameParams& f, int px, int py, const PixelUV& uv,
                                               unsigned* status, PixelCounters& pc) {
@@ -39,7 +40,7 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
     pray_init(r, o, d);
     TraceHit h;
     TraceCounters cnt;
-    const bool hit = trace_any<STATS, CHECKED, true, false>(w, coarse, cd, r, f.max_steps, h, cnt, status);
+    const bool hit = trace_any<STATS, CHECKED, true, false, SHARE>(w, coarse, cd, r, f.max_steps, h, cnt, status);
     if (STATS) {
         pc.v[0] += 1;
         pc.v[9] += 16;
@@ -72,7 +73,7 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
             PRay rs;
             pray_init_dir(rs, so, f.sun_d, f.sun_inv);
             TraceHit hs;
-            shadowed = trace_any<STATS, CHECKED, false, true>(w, coarse, cd, rs, f.shadow_max_steps, hs, cnt, status);
+            shadowed = trace_any<STATS, CHECKED, false, true, SHARE>(w, coarse, cd, rs, f.shadow_max_steps, hs, cnt, status);
             if (shadowed) flags |= VT_HIT_SHADOWED;
             if (STATS) {
                 pc.v[2] += 1;
@@ -98,7 +99,7 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
             PRay rb;
             pray_init(rb, so, bdir);
             TraceHit hb;
-            const bool bh = trace_any<STATS, CHECKED, false, true>(w, coarse, cd, rb, f.bounce_max_steps, hb, cnt, status);
+            const bool bh = trace_any<STATS, CHECKED, false, true, SHARE>(w, coarse, cd, rb, f.bounce_max_steps, hb, cnt, status);
             if (bh) flags |= VT_HIT_BOUNCE;
             bounce_open = !bh;
             if (STATS) {

@@ -363,6 +363,24 @@ struct Walker {
         return true;
     }
 
+    // The brick word wi.  SHARE: the lanes of the warp that look up a word
+    // at this point group by its index (__match_any_sync); one lane of each
+    // group loads it and passes it on (__shfl_sync).
+    template <bool SHARE>
+    __device__ __forceinline__ unsigned long long brick_word(const WorldView& w, unsigned i) const {
+#ifdef __CUDA_ARCH__
+        if (SHARE) {
+            const unsigned act = __activemask();
+            const unsigned peers = __match_any_sync(act, i);
+            const int leader = __ffs(peers) - 1;
+            unsigned long long v = 0ull;
+            if ((int)(threadIdx.x & 31u) == leader) v = __ldg(w.mask + i);
+            return __shfl_sync(peers, v, leader);
+        }
+#endif
+        return __ldg(w.mask + i);
+    }
+
     // One iteration: a lookup plus a jump, or a voxel test plus a unit step
     // (RUN: unit steps until the walk leaves the occupied brick).  In a warp
     // whose lanes are in different phases every iteration pays for both the
@@ -370,7 +388,8 @@ struct Walker {
     // loop pays the jump code once per brick visit instead (-4.5% on a 1080p
     // terrain frame of primary and shadow rays).
     // NEAR: the ray's origin passes near_origin (one-correction plane search).
-    template <bool MAT, bool RUN = true, bool NEAR = false>
+    // SHARE: brick words shared between the lanes of a warp (brick_word).
+    template <bool MAT, bool RUN = true, bool NEAR = false, bool SHARE = false>
     __device__ __forceinline__ int step(const WorldView& w, const unsigned char* cdist, TraceHit& h) {
         bool jump = false;
         int sh = 0, rad = 0;
@@ -391,7 +410,7 @@ struct Walker {
             }
             if (state == 1) {
                 wi = ci * 512u + ((unsigned)((c[0] >> 2) & 7) | ((unsigned)((c[1] >> 2) & 7) << 3) | ((unsigned)((c[2] >> 2) & 7) << 6));
-                word = __ldg(w.mask + wi);
+                word = brick_word<SHARE>(w, wi);
                 if (word == 0ull) {
                     jump = true;
                     sh = 2;
@@ -484,15 +503,109 @@ struct Walker {
         state = 0;
         return kMore;
     }
+
+    // The same walk with one code path for jumps and unit steps: every turn
+    // looks the cell up (unless it is in the occupied brick of the last turn),
+    // then leaves a box -- an empty chunk box, an empty brick box, or the one
+    // voxel that was tested -- by the same exit computation.  A warp whose
+    // lanes walk unrelated rays (the bounce pass) then runs one instruction
+    // stream for all of them instead of a jump path and a unit-run path; a
+    // unit step costs more than in step().  The lookup reads the chunk
+    // distance, the brick word and the brick distance without waiting on one
+    // another (the brick index is in range for any cell of the grid).
+    // Results are those of step() (every box exit is exact, see above); no
+    // material is read (the bounce pass needs none).
+    template <bool NEAR = false>
+    __device__ __forceinline__ int step_flat(const WorldView& w, const unsigned char* cdist, TraceHit& h) {
+        int sh = 0, rad = 1;
+        if (state != 2) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) c[i] = r.pos[i] ? nk[i] - 1 : nk[i];
+            const unsigned ci = (unsigned)(c[0] >> 5) + (unsigned)w.cdim[0] * ((unsigned)(c[1] >> 5) + (unsigned)w.cdim[1] * (unsigned)(c[2] >> 5));
+            wi = ci * 512u + ((unsigned)((c[0] >> 2) & 7) | ((unsigned)((c[1] >> 2) & 7) << 3) | ((unsigned)((c[2] >> 2) & 7) << 6));
+            const int dc = cdist[oct * w.cstride + ci];
+            word = __ldg(w.mask + wi);
+            const int bd = __ldg(w.bdist + (size_t)oct * w.nwords + wi);
+            if (dc) {
+                VT_STEP_HOOK(0);
+                sh = 5;
+                rad = dc;
+            } else if (word == 0ull) {
+                VT_STEP_HOOK(1);
+                sh = 2;
+                rad = bd;
+            } else {
+                vb = (unsigned)(c[0] & 3) | ((unsigned)(c[1] & 3) << 2) | ((unsigned)(c[2] & 3) << 4);
+                state = 2;
+            }
+        }
+        if (state == 2) {
+            VT_STEP_HOOK(2);
+            const unsigned half = (vb & 32u) ? (unsigned)(word >> 32) : (unsigned)word;
+            if ((half >> (vb & 31u)) & 1u) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) h.c[i] = r.pos[i] ? nk[i] - 1 : nk[i];
+                h.mat = 0u;
+                h.t = t;
+                h.axis = axis;
+                return kHit;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i) c[i] = r.pos[i] ? nk[i] - 1 : nk[i];
+        }
+        // leave the box: the voxel (sh 0), or the empty box reaching rad - 1
+        // units of 2^sh ahead of the unit of c
+        int K[3];
+        float tK[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int u = c[i] >> sh;
+            const int ri = (i == 1 && sh == 2) ? (int)((unsigned)(rad - 1) >> ((oct & 2u) ? 0 : kFlatYShift)) + 1 : rad;
+            K[i] = r.pos[i] ? (u + ri) * (1 << sh) : (u - (ri - 1)) * (1 << sh);
+            tK[i] = sh == 0 ? tm[i] : ptime(r, i, K[i]);
+        }
+        const int e = tK[0] < tK[1] ? (tK[0] < tK[2] ? 0 : 2) : (tK[1] < tK[2] ? 1 : 2);
+        const float T = e == 0 ? tK[0] : (e == 1 ? tK[1] : tK[2]);
+        int crossings = 0, kx = 0;
+        unsigned dv = 0;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            int cn = c[i];
+            if (i == e) {
+                cn = r.pos[i] ? K[i] : K[i] - 1;
+                kx = K[i];                                            // the plane crossed
+                dv = r.pos[i] ? (1u << (2 * i)) : 0u - (1u << (2 * i));  // the voxel's bit index moves by this
+            } else if (key_lt(tm[i], i, T, e)) {
+                cn = advance_axis<NEAR>(r, i, c[i], K[i], T, e);
+            }
+            crossings += abs(cn - c[i]);
+            if (cn != c[i]) {
+                nk[i] = r.pos[i] ? cn + 1 : cn;
+                tm[i] = ptime(r, i, nk[i]);
+            }
+            c[i] = cn;
+        }
+        n += crossings;
+        t = T;
+        axis = e;
+        if (n >= max_steps) return kMiss;
+        if ((unsigned)c[0] >= (unsigned)w.dims[0] || (unsigned)c[1] >= (unsigned)w.dims[1] ||
+            (unsigned)c[2] >= (unsigned)w.dims[2])
+            return kMiss;
+        // a unit step stays in the brick unless the crossed plane bounds it
+        if (sh == 0 && (kx & 3) != 0) vb += dv;
+        else state = 0;
+        return kMore;
+    }
 };
 
-template <bool MAT, bool RUN = true, bool NEAR = false>
+template <bool MAT, bool RUN = true, bool NEAR = false, bool SHARE = false>
 __device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned char* cdist, const PRay& r,
                                            int max_steps, TraceHit& h) {
     Walker wk;
     if (!wk.start(w, r.o, r.d, max_steps)) return false;
     int s;
-    while ((s = wk.step<MAT, RUN, NEAR>(w, cdist, h)) == Walker::kMore) {
+    while ((s = wk.step<MAT, RUN, NEAR, SHARE>(w, cdist, h)) == Walker::kMore) {
     }
     return s == Walker::kHit;
 }

@@ -1,11 +1,17 @@
 // tune.cu -- launch-configuration autotuner of the render kernels.
 //
-// The candidates are the warp-tile shapes (8x4, 16x2, 32x1 pixels) and
-// register budgets of the one-thread-per-pixel kernel, and the refill batch of
-// the persistent pixel-queue kernel.  All produce identical records; the tuner
-// times each on the caller's frame and keeps the fastest.  Choices can be
-// cached in a small text file, one line per key:
-//     <gpu name>|<X>x<Y>x<Z>|<W>x<H>|<rays>|<shade> <kernel> <tile w> <occupancy> <batch> <ms>
+// The search space: the warp-tile shape of the one-thread-per-pixel kernel (a
+// warp's pixel packet: 4x8, 8x4, 16x2 or 32x1 pixels) and its register budget,
+// lanes sharing brick-word loads, the refill batch of the persistent
+// pixel-queue kernel, an L2 persistence window over the brick words, and for
+// frames with bounce rays the deferred bounce walk (its refill threshold and
+// whether jumps and unit steps share one code path).  All produce identical
+// records; the tuner times candidates on the caller's frame in phases (launch
+// shape, then the L2 window, then the bounce pass, each phase keeping the
+// fastest so far) and keeps the fastest.  Brick (4^3) and chunk (32^3) sizes
+// are fixed by the data layout.  Choices can be cached in a small text file,
+// one line per key:
+//     <gpu name>|<X>x<Y>x<Z>|<W>x<H>|<rays>|<shade> <kernel> <tile w> <occupancy> <batch> <share> <l2> <refill> <walk> <ms>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -18,9 +24,14 @@
 namespace {
 
 bool valid(const vt_tuning& t) {
+    if (t.share_bricks < 0 || t.share_bricks > 1 || t.l2_persist < 0 || t.l2_persist > 1 || t.bounce_refill < 0 ||
+        t.bounce_refill > 32 || t.bounce_walk < 0 || t.bounce_walk > 1)
+        return false;
     if (t.kernel == VT_KERNEL_TILE || t.kernel == VT_KERNEL_PER_JOB)
-        return (t.warp_tile_w == 8 || t.warp_tile_w == 16 || t.warp_tile_w == 32) && (t.occupancy == 0 || t.occupancy == 1);
-    if (t.kernel == VT_KERNEL_QUEUE) return t.batch >= 1 && t.batch <= 32;
+        return (t.warp_tile_w == 4 || t.warp_tile_w == 8 || t.warp_tile_w == 16 || t.warp_tile_w == 32) &&
+               (t.occupancy == 0 || t.occupancy == 1) &&
+               (!t.share_bricks || (t.warp_tile_w == 8 && t.occupancy == 1));
+    if (t.kernel == VT_KERNEL_QUEUE) return t.batch >= 1 && t.batch <= 32 && !t.share_bricks;
     return false;
 }
 
@@ -43,7 +54,9 @@ bool cache_lookup(const char* path, const std::string& key, vt_tuning* t, float*
         std::string k;
         vt_tuning c;
         float m;
-        if (ls >> k >> c.kernel >> c.warp_tile_w >> c.occupancy >> c.batch >> m && k == key && valid(c)) {
+        if (ls >> k >> c.kernel >> c.warp_tile_w >> c.occupancy >> c.batch >> c.share_bricks >> c.l2_persist >>
+                c.bounce_refill >> c.bounce_walk >> m &&
+            k == key && valid(c)) {
             *t = c;
             *ms = m;
             found = true;  // the last record of a key wins
@@ -54,7 +67,8 @@ bool cache_lookup(const char* path, const std::string& key, vt_tuning* t, float*
 
 void cache_store(const char* path, const std::string& key, const vt_tuning& t, float ms) {
     std::ofstream out(path, std::ios::app);
-    out << key << ' ' << t.kernel << ' ' << t.warp_tile_w << ' ' << t.occupancy << ' ' << t.batch << ' ' << ms << '\n';
+    out << key << ' ' << t.kernel << ' ' << t.warp_tile_w << ' ' << t.occupancy << ' ' << t.batch << ' '
+        << t.share_bricks << ' ' << t.l2_persist << ' ' << t.bounce_refill << ' ' << t.bounce_walk << ' ' << ms << '\n';
 }
 
 // Read-bandwidth probe: each thread streams 16-byte words of the buffer with
@@ -153,11 +167,6 @@ vt_status vt_autotune(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, 
         if (best_ms) *best_ms = found_ms;
         return VT_OK;
     }
-    std::vector<vt_tuning> cands;
-    for (int tw : {8, 16, 32})
-        for (int occ : {0, 1}) cands.push_back(vt_tuning{VT_KERNEL_TILE, tw, occ, 16});
-    for (int b : {8, 16, 24}) cands.push_back(vt_tuning{VT_KERNEL_QUEUE, 8, 0, b});
-
     const size_t bytes = (size_t)cam->width * cam->height * sizeof(vt_hit);
     void* d_out = nullptr;
     vt_status s = ctx_scratch(ctx, bytes, &d_out);
@@ -169,7 +178,8 @@ vt_status vt_autotune(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, 
     vt_tuning win = saved;
     float win_ms = 0.0f;
     bool have = false;
-    for (const vt_tuning& c : cands) {
+    // times one candidate; keeps it if it is the fastest so far
+    auto trial = [&](const vt_tuning& c) {
         ctx->tuning = c;
         for (int i = 0; i < 2 && !s; ++i) s = vt_render(ctx, world, cam, params, (vt_hit*)d_out, ctx->stream);
         if (!s) s = check_cuda(ctx, cudaEventRecord(e0, ctx->stream), "cudaEventRecord");
@@ -178,13 +188,39 @@ vt_status vt_autotune(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, 
         if (!s) s = check_cuda(ctx, cudaEventSynchronize(e1), "cudaEventSynchronize");
         float ms = 0.0f;
         if (!s) s = check_cuda(ctx, cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
-        if (s) break;
+        if (s) return;
         ms /= (float)reps;
         if (!have || ms < win_ms) {
             win = c;
             win_ms = ms;
             have = true;
         }
+    };
+    // phase 1: the launch shape
+    std::vector<vt_tuning> cands;
+    for (int tw : {4, 8, 16, 32})
+        for (int occ : {0, 1}) cands.push_back(vt_tuning{VT_KERNEL_TILE, tw, occ, 16, 0, 0, 0, 0});
+    cands.push_back(vt_tuning{VT_KERNEL_TILE, 8, 1, 16, 1, 0, 0, 0});
+    for (int b : {8, 16, 24}) cands.push_back(vt_tuning{VT_KERNEL_QUEUE, 8, 0, b, 0, 0, 0, 0});
+    for (const vt_tuning& c : cands)
+        if (!s) trial(c);
+    // phase 2: the L2 persistence window over the brick words
+    if (!s) {
+        vt_tuning c = win;
+        c.l2_persist = 1;
+        trial(c);
+    }
+    // phase 3: the deferred bounce pass (frames with bounce rays through the tile kernel)
+    if (!s && (params->rays & VT_RAYS_BOUNCE) && win.kernel != VT_KERNEL_QUEUE) {
+        const vt_tuning base = win;
+        for (int walk : {0, 1})
+            for (int refill : {4, 8, 16}) {
+                if (walk == 0 && refill == 8) continue;  // the base's own (default) bounce pass
+                vt_tuning c = base;
+                c.bounce_walk = walk;
+                c.bounce_refill = refill;
+                if (!s) trial(c);
+            }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -99,7 +99,11 @@ struct vt_ctx {
     unsigned* d_work = nullptr;                  // ring of pixel-queue counters of the persistent kernels
     unsigned work_slot = 0;
     int persist_blocks = 0;                      // resident blocks per SM of the persistent render kernel
-    vt_tuning tuning = {VT_KERNEL_TILE, 8, 1, 16};
+    vt_tuning tuning = {VT_KERNEL_TILE, 8, 1, 16, 0, 0, 0, 0};
+    // the persisting-L2 set-aside has been requested (VT tuning l2_persist)
+    bool l2_setaside = false;
+    size_t l2_persist_max = 0;     // cudaDevAttrMaxPersistingL2CacheSize
+    size_t l2_window_max = 0;      // cudaDevAttrMaxAccessPolicyWindowSize
     // vt_render_host's pipeline: row bands rendered on band streams, each
     // copied to the host on the copy stream as soon as it is done (created on
     // first use)
@@ -121,7 +125,7 @@ struct vt_ctx {
     // screen tables of the frame sizes rendered so far (see screen_table)
     vt::ScreenTable screen[vt::kScreenTables];
     int n_screen = 0;
-    int bounce_blocks = 0;
+    int bounce_blocks[2] = {0, 0};     // resident blocks of the bounce walk kernels (brick-run, one-path)
 };
 
 namespace vt {
@@ -230,6 +234,18 @@ struct FrameParams;
 // (made on first use when `create` and the stream is not being captured;
 // *out stays null when none can be had).
 vt_status screen_table(vt_ctx* ctx, const FrameParams& f, cudaStream_t st, bool create, const float4** out);
+// While l2_window's guard lives, the kernels queued on its stream carry an
+// L2 access-policy window over a world's brick words (tuning l2_persist); the
+// stream's previous window comes back when the guard goes out of scope.
+struct L2Window {
+    cudaStream_t st = nullptr;
+    bool set = false;
+    cudaStreamAttrValue prev = {};
+    ~L2Window() {
+        if (set) cudaStreamSetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &prev);
+    }
+};
+vt_status l2_window(vt_ctx* ctx, const vt_world* world, cudaStream_t st, L2Window* guard);
 // The deferred bounce pass: queue buffers for `pixels` rays, and the trace +
 // shade kernels for a frame whose render kernel queued them.
 vt_status bounce_buffers(vt_ctx* ctx, size_t pixels);
