@@ -307,6 +307,29 @@ def _timed_flushed(torch, fn, reps: int, flush) -> float:
     return ms / reps
 
 
+def measure_config1_frames(vt, ctx, torch, flush) -> dict:
+    """The headline frames alone (the 512x256x512 world, its 8 cameras at
+    1920x1080, primary + shadow): 2 warm-up frames, then the 8 cameras once
+    each after an L2 flush.  For profiling a tuning (--only config1 --tuning)."""
+    _, mats, cams, params = setup_scene(vt, 0)
+    w = vt.World(ctx, WORLD)
+    w.upload_dense(mats)
+    out = ctx.alloc(IMAGE[0] * IMAGE[1] * 16)
+    sh = torch.cuda.current_stream().cuda_stream
+    ms = []
+    for i in range(2 + CAMERAS):
+        def frame():
+            ctx.check(ctx.lib.vt_render(ctx.handle, w.handle, C.byref(cams[i % CAMERAS]), C.byref(params), out.ptr,
+                                        sh))
+        if i < 2:
+            frame()
+        else:
+            ms.append(_timed_flushed(torch, frame, 1, flush))
+    w.close()
+    out.free()
+    return {"workload": workload_config()["workload"], "ms_per_frame": sum(ms) / len(ms), "tuning": ctx.get_tuning()}
+
+
 def measure_config0(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py) -> dict:
     """128^3 terrain, 640x360 primary rays (max 512 steps): the small plain
     scene that the CPU oracle also renders whole."""
@@ -783,8 +806,10 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the other workloads' measurements that follow the headline")
-    ap.add_argument("--only", choices=["config0", "config2", "config3", "config4"],
-                    help="run just one of the other workloads and print its result (for profiling)")
+    ap.add_argument("--only", choices=["config0", "config1", "config2", "config3", "config4"],
+                    help="run just one workload and print its result (for profiling)")
+    ap.add_argument("--tuning", default="",
+                    help="with --only: vt_tuning fields for the context, e.g. share_bricks=1,l2_persist=1")
     args = ap.parse_args()
     if args.only:
         import torch
@@ -795,9 +820,12 @@ def main() -> None:
         import scenes
         import vt
         ctx = vt.Context(0)
+        if args.tuning:
+            ctx.set_tuning(**{k: int(v) for k, v in (kv.split("=") for kv in args.tuning.split(","))})
         peak, kind = read_peaks()
         flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
         fn = {"config0": lambda: measure_config0(vt, scenes, ctx, torch, flush, peak, kind, oracle_py),
+              "config1": lambda: measure_config1_frames(vt, ctx, torch, flush),
               "config2": lambda: measure_config2(vt, scenes, ctx, torch, flush, peak, kind, oracle_py),
               "config3": lambda: measure_config3(vt, scenes, ctx, torch, peak, kind, oracle_py),
               "config4": lambda: measure_config4(vt, scenes, ctx, torch, peak, kind, oracle_py)}[args.only]
