@@ -81,16 +81,11 @@ cudaError_t host_free(void* p) {
     return e;
 }
 
-vt_status l2_window(vt_ctx* ctx, const vt_world* world, cudaStream_t st, L2Window* guard) {
-    if (!ctx->tuning.l2_persist || !st) return VT_OK;   // (the legacy default stream takes no attributes)
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
-        cudaGetLastError();
-        return VT_OK;
-    }
+vt_status l2_policy(vt_ctx* ctx, const vt_world* world, cudaAccessPolicyWindow* storage,
+                    const cudaAccessPolicyWindow** out) {
+    *out = nullptr;
+    if (!ctx->tuning.l2_persist) return VT_OK;
     if (!ctx->l2_setaside) {
-        // the persisting set-aside of this process's context (undone when the
-        // context goes; nothing outlasts the process)
         int maxp = 0, maxw = 0;
         VT_CUDA(ctx, cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, ctx->device));
         VT_CUDA(ctx, cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device));
@@ -100,18 +95,15 @@ vt_status l2_window(vt_ctx* ctx, const vt_world* world, cudaStream_t st, L2Windo
         ctx->l2_setaside = true;
     }
     if (!ctx->l2_persist_max || !ctx->l2_window_max) return VT_OK;
-    VT_CUDA(ctx, cudaStreamGetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &guard->prev));
     const size_t words = world->nchunks * (size_t)kBricksPerChunk * 8u;
     const size_t bytes = words < ctx->l2_window_max ? words : ctx->l2_window_max;
-    cudaStreamAttrValue v = {};
-    v.accessPolicyWindow.base_ptr = world->d_mask;
-    v.accessPolicyWindow.num_bytes = bytes;
-    v.accessPolicyWindow.hitRatio = bytes <= ctx->l2_persist_max ? 1.0f : (float)ctx->l2_persist_max / (float)bytes;
-    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    VT_CUDA(ctx, cudaStreamSetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &v));
-    guard->st = st;
-    guard->set = true;
+    *storage = cudaAccessPolicyWindow{};
+    storage->base_ptr = world->d_mask;
+    storage->num_bytes = bytes;
+    storage->hitRatio = bytes <= ctx->l2_persist_max ? 1.0f : (float)ctx->l2_persist_max / (float)bytes;
+    storage->hitProp = cudaAccessPropertyPersisting;
+    storage->missProp = cudaAccessPropertyStreaming;
+    *out = storage;
     return VT_OK;
 }
 

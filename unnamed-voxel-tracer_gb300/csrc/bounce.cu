@@ -2,6 +2,7 @@
 // kernel that traces the queued bounce rays with per-lane refill, and a kernel
 // that shades the pixels whose bounce ray was deferred.
 #include "bounce.cuh"
+#include "launch.cuh"
 #include "trace_p.cuh"
 
 namespace vt {
@@ -119,13 +120,18 @@ vt_status launch_bounce(vt_ctx* ctx, const vt_world* world, const FrameParams& f
         ctx->bounce_blocks[flat] = ctx->sm_count * (nb > 0 ? nb : 1);
     }
     const BounceJob* jobs = reinterpret_cast<const BounceJob*>(ctx->d_bounce_jobs);
+    cudaAccessPolicyWindow win_storage;
+    const cudaAccessPolicyWindow* win = nullptr;  // L2 window over the brick words (tuning l2_persist)
+    vt_status s = l2_policy(ctx, world, &win_storage, &win);
+    if (s) return s;
     if (flat)
-        k_bounce_trace<true><<<ctx->bounce_blocks[1], kBounceBlock, 0, st>>>(
-            w, jobs, ctx->d_bounce_ctr, ctx->d_bounce_ctr + 1, ctx->d_bounce_open, f.bounce_max_steps, refill);
+        VT_CUDA(ctx, launch_kernel(k_bounce_trace<true>, dim3(ctx->bounce_blocks[1]), dim3(kBounceBlock), 0, st, win, w,
+                                   jobs, (const unsigned*)ctx->d_bounce_ctr, ctx->d_bounce_ctr + 1, ctx->d_bounce_open,
+                                   f.bounce_max_steps, refill));
     else
-        k_bounce_trace<false><<<ctx->bounce_blocks[0], kBounceBlock, 0, st>>>(
-            w, jobs, ctx->d_bounce_ctr, ctx->d_bounce_ctr + 1, ctx->d_bounce_open, f.bounce_max_steps, refill);
-    VT_CUDA(ctx, cudaGetLastError());
+        VT_CUDA(ctx, launch_kernel(k_bounce_trace<false>, dim3(ctx->bounce_blocks[0]), dim3(kBounceBlock), 0, st, win, w,
+                                   jobs, (const unsigned*)ctx->d_bounce_ctr, ctx->d_bounce_ctr + 1, ctx->d_bounce_open,
+                                   f.bounce_max_steps, refill));
     k_bounce_finish<<<ctx->sm_count * 8, kBounceBlock, 0, st>>>(w, f, jobs, ctx->d_bounce_ctr, ctx->d_bounce_open,
                                                                 d_out);
     VT_CUDA(ctx, cudaGetLastError());

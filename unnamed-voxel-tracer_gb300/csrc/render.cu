@@ -10,6 +10,7 @@
 // record; nothing goes through memory between the passes.
 #include <cstring>
 
+#include "launch.cuh"
 #include "render_pixel.cuh"
 
 namespace vt {
@@ -416,9 +417,10 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
     }
     const size_t sm = use_smem ? smem : 0;
     const vt_tuning& tu = ctx->tuning;
-    L2Window l2;  // restores the stream's access-policy window when the launches are queued
+    cudaAccessPolicyWindow win_storage;
+    const cudaAccessPolicyWindow* win = nullptr;  // L2 window over the brick words (tuning l2_persist)
     {
-        vt_status s = l2_window(ctx, world, stream, &l2);
+        vt_status s = l2_policy(ctx, world, &win_storage, &win);
         if (s) return s;
     }
     if (!stats && !checked && tu.kernel == VT_KERNEL_QUEUE) {
@@ -436,10 +438,11 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         const unsigned blocks = (unsigned)(ctx->sm_count * ctx->persist_blocks);
         const int batch = tu.batch;
         if (near_origin(f.pos))
-            k_render_persist<true><<<blocks, kPersistBlock, 0, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
+            VT_CUDA(ctx, launch_kernel(k_render_persist<true>, dim3(blocks), dim3(kPersistBlock), 0, stream, win, w, f,
+                                       d_out, counter, total, tiles_x, batch));
         else
-            k_render_persist<false><<<blocks, kPersistBlock, 0, stream>>>(w, f, d_out, counter, total, tiles_x, batch);
-        VT_CUDA(ctx, cudaGetLastError());
+            VT_CUDA(ctx, launch_kernel(k_render_persist<false>, dim3(blocks), dim3(kPersistBlock), 0, stream, win, w,
+                                       f, d_out, counter, total, tiles_x, batch));
         return VT_OK;
     }
     {
@@ -455,10 +458,12 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         f.bounce_jobs = ctx->d_bounce_jobs;
         f.bounce_count = ctx->d_bounce_ctr;
     }
+    cudaError_t le = cudaSuccess;
 #define VT_LAUNCH_X(S, C, M, TW, O, SH)                                                                         \
-    k_render<S, C, M, TW, O, SH><<<dim3((cam->width + BlockTile<TW>::kW - 1) / BlockTile<TW>::kW,               \
-                                        (rows + BlockTile<TW>::kH - 1) / BlockTile<TW>::kH),                    \
-                                   kBlock, sm, stream>>>(w, f, d_out, ctx->d_status, ctx->d_counters)
+    le = launch_kernel(k_render<S, C, M, TW, O, SH>,                                                            \
+                       dim3((cam->width + BlockTile<TW>::kW - 1) / BlockTile<TW>::kW,                           \
+                            (rows + BlockTile<TW>::kH - 1) / BlockTile<TW>::kH),                                \
+                       dim3(kBlock), sm, stream, win, w, f, d_out, ctx->d_status, ctx->d_counters)
 #define VT_LAUNCH(S, C, M, TW, O) VT_LAUNCH_X(S, C, M, TW, O, false)
 #define VT_LAUNCH_M(S, C, TW, O)      \
     if (use_smem) VT_LAUNCH(S, C, true, TW, O); \
@@ -484,7 +489,7 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
 #undef VT_LAUNCH_M
 #undef VT_LAUNCH
 #undef VT_LAUNCH_X
-    VT_CUDA(ctx, cudaGetLastError());
+    VT_CUDA(ctx, le);
     if (stats || checked) return note_status_writer(ctx, stream);  // the model walk checks its indexes
     if (defer) return launch_bounce(ctx, world, f, d_out, stream);
     return VT_OK;

@@ -234,18 +234,13 @@ struct FrameParams;
 // (made on first use when `create` and the stream is not being captured;
 // *out stays null when none can be had).
 vt_status screen_table(vt_ctx* ctx, const FrameParams& f, cudaStream_t st, bool create, const float4** out);
-// While l2_window's guard lives, the kernels queued on its stream carry an
-// L2 access-policy window over a world's brick words (tuning l2_persist); the
-// stream's previous window comes back when the guard goes out of scope.
-struct L2Window {
-    cudaStream_t st = nullptr;
-    bool set = false;
-    cudaStreamAttrValue prev = {};
-    ~L2Window() {
-        if (set) cudaStreamSetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &prev);
-    }
-};
-vt_status l2_window(vt_ctx* ctx, const vt_world* world, cudaStream_t st, L2Window* guard);
+// The L2 access-policy window over a world's brick words that render
+// launches carry as a launch attribute (tuning l2_persist).  *out is null when
+// the tuning is off or the device has no persisting L2; the first use
+// reserves the device's persisting L2 for this process's context (undone
+// when the context is destroyed).
+vt_status l2_policy(vt_ctx* ctx, const vt_world* world, cudaAccessPolicyWindow* storage,
+                    const cudaAccessPolicyWindow** out);
 // The deferred bounce pass: queue buffers for `pixels` rays, and the trace +
 // shade kernels for a frame whose render kernel queued them.
 vt_status bounce_buffers(vt_ctx* ctx, size_t pixels);
