@@ -234,7 +234,8 @@ def test_bounce_rays(vt, oracle, ctx):
 
 
 BOUNCE_TUNINGS = [dict(bounce_walk=wk, bounce_refill=r) for wk in (0, 1) for r in (0, 1, 4, 16, 32)] + \
-                 [dict(bounce_walk=1, l2_persist=1), dict(warp_tile_w=4, bounce_walk=1, bounce_refill=8)]
+                 [dict(bounce_walk=1, l2_persist=1), dict(warp_tile_w=4, bounce_walk=1, bounce_refill=8)] + \
+                 [dict(bounce_sort=1, warp_tile_w=tw, bounce_walk=wk) for tw in (4, 8, 16, 32) for wk in (0, 1)]
 
 
 @pytest.mark.parametrize("tuning", BOUNCE_TUNINGS, ids=lambda t: "-".join(f"{k}{v}" for k, v in t.items()))
@@ -250,6 +251,24 @@ def test_bounce_pass_variants(vt, oracle, tuned, tuning):
     gpu, ref, _ = render_both(vt, oracle, tuned, mats, cam, p)
     compare(gpu, ref)
     assert (gpu["flags"] & vt.HIT_BOUNCE).any() and ((gpu["flags"] & 5) == 1).any()
+
+
+def test_binned_bounce_pass_across_frame_sizes(vt, tuned):
+    """The direction-binned bounce pass keeps a frame's rays in per-thread
+    slots tagged with the frame: frames of different sizes in a row (slots
+    of earlier frames left in place) equal the default pass."""
+    d = vt.gen_desc((256, 128, 256), seed=13, trees=40, caves=True)
+    w = make_world(vt, tuned, vt.gen_world(d))
+    p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW | vt.RAYS_BOUNCE, seed=9, sun_dir=vt.gen_sun(13))
+    try:
+        cams = [vt.gen_camera(d, c, W, H) for c, (W, H) in enumerate([(640, 360), (97, 61), (640, 360), (333, 500)])]
+        want = [vt.render_host(tuned, w, cam, p) for cam in cams]
+        tuned.set_tuning(bounce_sort=1)
+        for _ in range(2):
+            for cam, ref in zip(cams, want):
+                assert np.array_equal(vt.render_host(tuned, w, cam, p), ref)
+    finally:
+        w.close()
 
 
 def test_lambert_and_checked_variant(vt, oracle, ctx):

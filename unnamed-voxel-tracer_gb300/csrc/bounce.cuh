@@ -21,14 +21,29 @@ struct BounceJob {
     float o[3];
     float d[3];
     unsigned pixel;
-    unsigned pad;
+    unsigned tag;  // the frame number in per-thread slots (FrameParams::bounce_tag), else unused
 };
 static_assert(sizeof(BounceJob) == 32, "bounce job layout");
 
 // Appends one bounce ray; called by the lanes of a warp that have one, with
-// the warp possibly diverged (one atomic per converged group).
+// the warp possibly diverged (one atomic per converged group).  With a frame
+// tag the ray goes to the calling thread's own slot instead (its index in
+// the launch grid, so that slot order is image-tile order), tagged.
 __device__ __forceinline__ void append_bounce(const FrameParams& f, const float o[3], const float d[3],
                                               unsigned pixel) {
+    if (f.bounce_tag) {
+        const size_t slot = ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+        BounceJob* j = reinterpret_cast<BounceJob*>(f.bounce_jobs) + slot;
+        j->o[0] = o[0];
+        j->o[1] = o[1];
+        j->o[2] = o[2];
+        j->d[0] = d[0];
+        j->d[1] = d[1];
+        j->d[2] = d[2];
+        j->pixel = pixel;
+        j->tag = f.bounce_tag;
+        return;
+    }
     const unsigned act = __activemask();
     const unsigned lane = threadIdx.x & 31u;
     const int leader = __ffs(act) - 1;

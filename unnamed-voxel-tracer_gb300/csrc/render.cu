@@ -301,6 +301,7 @@ FrameParams make_frame(const vt_camera* cam, const vt_params* p) {
     f.row_end = cam->height;
     f.bounce_jobs = nullptr;
     f.bounce_count = nullptr;
+    f.bounce_tag = 0;
     f.screen = nullptr;
     f.max_steps = p->max_steps;
     f.shadow_max_steps = p->shadow_max_steps;
@@ -450,13 +451,29 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         if (s) return s;
     }
     const bool defer = allow_defer && (p->rays & VT_RAYS_BOUNCE) && !stats && !checked;
+    size_t nslots = 0;
     if (defer) {
         vt_status s = bounce_buffers(ctx, (size_t)cam->width * (size_t)cam->height);
         if (s) return s;
+        if (tu.bounce_sort) {
+            // one slot per thread of the launch below
+            const int tw = tu.warp_tile_w == 4 ? 4 : (tu.warp_tile_w == 16 ? 16 : (tu.warp_tile_w == 32 ? 32 : 8));
+            const int bw = tw == 4 ? BlockTile<4>::kW : (tw == 16 ? BlockTile<16>::kW : (tw == 32 ? BlockTile<32>::kW : BlockTile<8>::kW));
+            const int bh = tw == 4 ? BlockTile<4>::kH : (tw == 16 ? BlockTile<16>::kH : (tw == 32 ? BlockTile<32>::kH : BlockTile<8>::kH));
+            nslots = (size_t)((cam->width + bw - 1) / bw) * (size_t)((rows + bh - 1) / bh) * kBlock;
+            s = bounce_slots(ctx, nslots);
+            if (s) return s;
+        }
         VT_CUDA(ctx, cudaStreamWaitEvent(stream, ctx->ev_bounce, 0));
         VT_CUDA(ctx, cudaMemsetAsync(ctx->d_bounce_ctr, 0, 2 * sizeof(unsigned), stream));
-        f.bounce_jobs = ctx->d_bounce_jobs;
         f.bounce_count = ctx->d_bounce_ctr;
+        if (nslots) {
+            if (++ctx->bounce_tag == 0) ctx->bounce_tag = 1;  // (0 means "no tag")
+            f.bounce_jobs = ctx->d_bounce_slots;
+            f.bounce_tag = ctx->bounce_tag;
+        } else {
+            f.bounce_jobs = ctx->d_bounce_jobs;
+        }
     }
     cudaError_t le = cudaSuccess;
 #define VT_LAUNCH_X(S, C, M, TW, O, SH)                                                                         \
@@ -491,7 +508,7 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
 #undef VT_LAUNCH_X
     VT_CUDA(ctx, le);
     if (stats || checked) return note_status_writer(ctx, stream);  // the model walk checks its indexes
-    if (defer) return launch_bounce(ctx, world, f, d_out, stream);
+    if (defer) return launch_bounce(ctx, world, f, d_out, stream, nslots);
     return VT_OK;
 }
 

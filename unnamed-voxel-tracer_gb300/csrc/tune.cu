@@ -11,7 +11,7 @@
 // fastest so far) and keeps the fastest.  Brick (4^3) and chunk (32^3) sizes
 // are fixed by the data layout.  Choices can be cached in a small text file,
 // one line per key:
-//     <gpu name>|<X>x<Y>x<Z>|<W>x<H>|<rays>|<shade> <kernel> <tile w> <occupancy> <batch> <share> <l2> <refill> <walk> <ms>
+//     <gpu name>|<X>x<Y>x<Z>|<W>x<H>|<rays>|<shade> <kernel> <tile w> <occupancy> <batch> <share> <l2> <refill> <walk> <sort> <ms>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -25,7 +25,7 @@ namespace {
 
 bool valid(const vt_tuning& t) {
     if (t.share_bricks < 0 || t.share_bricks > 1 || t.l2_persist < 0 || t.l2_persist > 1 || t.bounce_refill < 0 ||
-        t.bounce_refill > 32 || t.bounce_walk < 0 || t.bounce_walk > 1)
+        t.bounce_refill > 32 || t.bounce_walk < 0 || t.bounce_walk > 1 || t.bounce_sort < 0 || t.bounce_sort > 1)
         return false;
     if (t.kernel == VT_KERNEL_TILE || t.kernel == VT_KERNEL_PER_JOB)
         return (t.warp_tile_w == 4 || t.warp_tile_w == 8 || t.warp_tile_w == 16 || t.warp_tile_w == 32) &&
@@ -55,7 +55,7 @@ bool cache_lookup(const char* path, const std::string& key, vt_tuning* t, float*
         vt_tuning c;
         float m;
         if (ls >> k >> c.kernel >> c.warp_tile_w >> c.occupancy >> c.batch >> c.share_bricks >> c.l2_persist >>
-                c.bounce_refill >> c.bounce_walk >> m &&
+                c.bounce_refill >> c.bounce_walk >> c.bounce_sort >> m &&
             k == key && valid(c)) {
             *t = c;
             *ms = m;
@@ -68,7 +68,8 @@ bool cache_lookup(const char* path, const std::string& key, vt_tuning* t, float*
 void cache_store(const char* path, const std::string& key, const vt_tuning& t, float ms) {
     std::ofstream out(path, std::ios::app);
     out << key << ' ' << t.kernel << ' ' << t.warp_tile_w << ' ' << t.occupancy << ' ' << t.batch << ' '
-        << t.share_bricks << ' ' << t.l2_persist << ' ' << t.bounce_refill << ' ' << t.bounce_walk << ' ' << ms << '\n';
+        << t.share_bricks << ' ' << t.l2_persist << ' ' << t.bounce_refill << ' ' << t.bounce_walk << ' '
+        << t.bounce_sort << ' ' << ms << '\n';
 }
 
 // Read-bandwidth probe: each thread streams 16-byte words of the buffer with
@@ -199,9 +200,9 @@ vt_status vt_autotune(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, 
     // phase 1: the launch shape
     std::vector<vt_tuning> cands;
     for (int tw : {4, 8, 16, 32})
-        for (int occ : {0, 1}) cands.push_back(vt_tuning{VT_KERNEL_TILE, tw, occ, 16, 0, 0, 0, 0});
-    cands.push_back(vt_tuning{VT_KERNEL_TILE, 8, 1, 16, 1, 0, 0, 0});
-    for (int b : {8, 16, 24}) cands.push_back(vt_tuning{VT_KERNEL_QUEUE, 8, 0, b, 0, 0, 0, 0});
+        for (int occ : {0, 1}) cands.push_back(vt_tuning{VT_KERNEL_TILE, tw, occ, 16, 0, 0, 0, 0, 0});
+    cands.push_back(vt_tuning{VT_KERNEL_TILE, 8, 1, 16, 1, 0, 0, 0, 0});
+    for (int b : {8, 16, 24}) cands.push_back(vt_tuning{VT_KERNEL_QUEUE, 8, 0, b, 0, 0, 0, 0, 0});
     for (const vt_tuning& c : cands)
         if (!s) trial(c);
     // phase 2: the L2 persistence window over the brick words
@@ -213,14 +214,16 @@ vt_status vt_autotune(vt_ctx* ctx, const vt_world* world, const vt_camera* cam, 
     // phase 3: the deferred bounce pass (frames with bounce rays through the tile kernel)
     if (!s && (params->rays & VT_RAYS_BOUNCE) && win.kernel != VT_KERNEL_QUEUE) {
         const vt_tuning base = win;
-        for (int walk : {0, 1})
-            for (int refill : {4, 8, 16}) {
-                if (walk == 0 && refill == 8) continue;  // the base's own (default) bounce pass
-                vt_tuning c = base;
-                c.bounce_walk = walk;
-                c.bounce_refill = refill;
-                if (!s) trial(c);
-            }
+        for (int sort : {0, 1})
+            for (int walk : {0, 1})
+                for (int refill : {4, 8, 16}) {
+                    if (sort == 0 && walk == 0 && refill == 8) continue;  // the base's own (default) bounce pass
+                    vt_tuning c = base;
+                    c.bounce_sort = sort;
+                    c.bounce_walk = walk;
+                    c.bounce_refill = refill;
+                    if (!s) trial(c);
+                }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -62,7 +62,7 @@ class Stats_t(C.Structure):
 class Tuning_t(C.Structure):
     _fields_ = [("kernel", C.c_int32), ("warp_tile_w", C.c_int32), ("occupancy", C.c_int32), ("batch", C.c_int32),
                 ("share_bricks", C.c_int32), ("l2_persist", C.c_int32), ("bounce_refill", C.c_int32),
-                ("bounce_walk", C.c_int32)]
+                ("bounce_walk", C.c_int32), ("bounce_sort", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -256,8 +256,9 @@ class Context:
 
     def set_tuning(self, kernel: int = KERNEL_TILE, warp_tile_w: int = 8, occupancy: int = 1,
                    batch: int = 16, share_bricks: int = 0, l2_persist: int = 0, bounce_refill: int = 0,
-                   bounce_walk: int = 0) -> None:
-        t = Tuning_t(kernel, warp_tile_w, occupancy, batch, share_bricks, l2_persist, bounce_refill, bounce_walk)
+                   bounce_walk: int = 0, bounce_sort: int = 0) -> None:
+        t = Tuning_t(kernel, warp_tile_w, occupancy, batch, share_bricks, l2_persist, bounce_refill, bounce_walk,
+                     bounce_sort)
         self.check(self.lib.vt_set_tuning(self.handle, C.byref(t)))
 
     def get_tuning(self) -> dict:
