@@ -448,8 +448,9 @@ typedef struct {
     int32_t bounce_refill; /* deferred bounce rays: idle lanes (1..32) that make a warp refill; 0 = 8 */
     int32_t bounce_walk;   /* deferred bounce rays: 0 = brick-run walk (unit steps of an occupied brick
                               in an inner loop), 1 = one advance per turn for jumps and unit steps alike */
-    int32_t bounce_sort;   /* deferred bounce rays: 1 = queued by image strip and grouped by direction
-                              (per-thread slots, then a binning kernel) instead of in append order */
+    int32_t bounce_sort;   /* deferred bounce rays: 1 = each 16x16-pixel block of the frame kernel appends
+                              its rays sorted by direction (8x4 capped tiles without share_bricks; other
+                              shapes append in order) */
 } vt_tuning;
 vt_status vt_set_tuning(vt_ctx* ctx, const vt_tuning* tuning);
 vt_status vt_get_tuning(vt_ctx* ctx, vt_tuning* tuning);

@@ -254,9 +254,9 @@ def test_bounce_pass_variants(vt, oracle, tuned, tuning):
 
 
 def test_binned_bounce_pass_across_frame_sizes(vt, tuned):
-    """The direction-binned bounce pass keeps a frame's rays in per-thread
-    slots tagged with the frame: frames of different sizes in a row (slots
-    of earlier frames left in place) equal the default pass."""
+    """The direction-sorted bounce append (each frame-kernel block sorts its
+    rays in shared memory and appends them with one atomic): frames of
+    different sizes, ragged edge blocks included, equal the default pass."""
     d = vt.gen_desc((256, 128, 256), seed=13, trees=40, caves=True)
     w = make_world(vt, tuned, vt.gen_world(d))
     p = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW | vt.RAYS_BOUNCE, seed=9, sun_dir=vt.gen_sun(13))

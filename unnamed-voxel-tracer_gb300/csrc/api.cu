@@ -226,7 +226,6 @@ vt_status vt_ctx_destroy(vt_ctx* ctx) {
     if (ctx->h_status) host_free(ctx->h_status);
     if (ctx->ev_status) cudaEventDestroy(ctx->ev_status);
     dev_free(ctx->d_bounce_jobs);
-    dev_free(ctx->d_bounce_slots);
     dev_free(ctx->d_bounce_open);
     dev_free(ctx->d_bounce_ctr);
     if (ctx->ev_bounce) cudaEventDestroy(ctx->ev_bounce);

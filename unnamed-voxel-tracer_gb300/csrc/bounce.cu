@@ -63,85 +63,6 @@ __global__ void __launch_bounds__(kBounceBlock) k_bounce_trace(WorldView w, cons
     }
 }
 
-// Direction binning of the bounce rays (tuning bounce_sort).  The frame
-// kernel wrote each ray to its thread's slot, so a run of kBinSeg slots is a
-// strip of image tiles (128 x 16 pixels for 8 x 4 warp tiles).  One block per
-// run keeps the slots tagged with this frame, sorts them by direction class
-// (the cube-map face of the direction and a 4 x 4 cell on it, 96 classes) in
-// shared memory, and appends them to the queue in that order: consecutive
-// queue entries then start close together and head the same way, so the
-// lanes of a warp in the trace kernel walk similar paths.
-constexpr int kBinSeg = 2048;
-constexpr int kBinBlock = 256;
-constexpr int kBins = 96;
-constexpr int kBinPer = kBinSeg / kBinBlock;
-
-__device__ __forceinline__ unsigned direction_bin(const float d[3]) {
-    const float ax = fabsf(d[0]), ay = fabsf(d[1]), az = fabsf(d[2]);
-    float m = ax, u = d[1], v = d[2], s = d[0];
-    unsigned face = 0;
-    if (ay > m && ay >= az) {
-        m = ay; u = d[0]; v = d[2]; s = d[1]; face = 2;
-    } else if (az > m && az > ay) {
-        m = az; u = d[0]; v = d[1]; s = d[2]; face = 4;
-    }
-    if (s < 0.0f) face += 1;
-    const float iu = (u / m + 1.0f) * 2.0f, iv = (v / m + 1.0f) * 2.0f;   // [0, 4]
-    const unsigned cu = iu >= 3.0f ? 3u : (iu >= 2.0f ? 2u : (iu >= 1.0f ? 1u : 0u));
-    const unsigned cv = iv >= 3.0f ? 3u : (iv >= 2.0f ? 2u : (iv >= 1.0f ? 1u : 0u));
-    return face * 16u + cu * 4u + cv;
-}
-
-__global__ void __launch_bounds__(kBinBlock) k_bounce_bin(const BounceJob* __restrict__ slots, unsigned nslots,
-                                                          unsigned tag, BounceJob* __restrict__ queue,
-                                                          unsigned* __restrict__ counters) {
-    extern __shared__ uint4 s_raw[];  // kBinSeg jobs, two uint4 each
-    __shared__ unsigned s_hist[kBins], s_base;
-    const BounceJob* s_jobs = reinterpret_cast<const BounceJob*>(s_raw);
-    const unsigned seg = blockIdx.x * (unsigned)kBinSeg;
-    const unsigned n = min((unsigned)kBinSeg, nslots - seg);
-    const uint4* src = reinterpret_cast<const uint4*>(slots + seg);
-    for (unsigned i = threadIdx.x; i < 2u * n; i += kBinBlock) s_raw[i] = src[i];
-    for (unsigned i = threadIdx.x; i < (unsigned)kBins; i += kBinBlock) s_hist[i] = 0u;
-    __syncthreads();
-    unsigned bin[kBinPer], rank[kBinPer];
-#pragma unroll
-    for (int k = 0; k < kBinPer; ++k) {
-        const unsigned i = threadIdx.x + (unsigned)k * kBinBlock;
-        bin[k] = 0xFFFFFFFFu;
-        if (i < n && s_jobs[i].tag == tag) {
-            bin[k] = direction_bin(s_jobs[i].d);
-            rank[k] = atomicAdd(&s_hist[bin[k]], 1u);
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        // exclusive scan of the 96 class counts, 3 per lane
-        const unsigned l = threadIdx.x;
-        const unsigned a = s_hist[3 * l], b = s_hist[3 * l + 1], c = s_hist[3 * l + 2];
-        unsigned incl = a + b + c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if ((int)l >= o) incl += v;
-        }
-        const unsigned excl = incl - (a + b + c);
-        s_hist[3 * l] = excl;
-        s_hist[3 * l + 1] = excl + a;
-        s_hist[3 * l + 2] = excl + a + b;
-        const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        if (l == 31) s_base = total ? atomicAdd(counters, total) : 0u;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < kBinPer; ++k) {
-        if (bin[k] != 0xFFFFFFFFu) {
-            const unsigned i = threadIdx.x + (unsigned)k * kBinBlock;
-            queue[s_base + s_hist[bin[k]] + rank[k]] = s_jobs[i];
-        }
-    }
-}
-
 // One thread per deferred pixel: the shading render_pixel would have done with
 // this bounce result, and the record's rgba and VT_HIT_BOUNCE flag.
 __global__ void __launch_bounds__(kBounceBlock) k_bounce_finish(WorldView w, FrameParams f,
@@ -188,33 +109,8 @@ vt_status bounce_buffers(vt_ctx* ctx, size_t pixels) {
     return VT_OK;
 }
 
-vt_status bounce_slots(vt_ctx* ctx, size_t slots) {
-    if (slots <= ctx->bounce_slot_capacity) return VT_OK;
-    VT_CUDA(ctx, cudaDeviceSynchronize());
-    vt::dev_free(ctx->d_bounce_slots);
-    ctx->d_bounce_slots = nullptr;
-    ctx->bounce_slot_capacity = 0;
-    VT_CUDA(ctx, vt::dev_alloc(&ctx->d_bounce_slots, slots * sizeof(BounceJob)));
-    VT_CUDA(ctx, cudaMemset(ctx->d_bounce_slots, 0, slots * sizeof(BounceJob)));  // tag 0: no ray
-    ctx->bounce_slot_capacity = slots;
-    return VT_OK;
-}
-
-vt_status launch_bounce(vt_ctx* ctx, const vt_world* world, const FrameParams& f, uint4* d_out, cudaStream_t st,
-                        size_t nslots) {
+vt_status launch_bounce(vt_ctx* ctx, const vt_world* world, const FrameParams& f, uint4* d_out, cudaStream_t st) {
     const WorldView w = world->view();
-    if (nslots) {
-        if (!ctx->bin_smem_set) {
-            VT_CUDA(ctx, cudaFuncSetAttribute(k_bounce_bin, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              kBinSeg * (int)sizeof(BounceJob)));
-            ctx->bin_smem_set = true;
-        }
-        const unsigned blocks = (unsigned)((nslots + kBinSeg - 1) / kBinSeg);
-        k_bounce_bin<<<blocks, kBinBlock, kBinSeg * sizeof(BounceJob), st>>>(
-            reinterpret_cast<const BounceJob*>(ctx->d_bounce_slots), (unsigned)nslots, f.bounce_tag,
-            reinterpret_cast<BounceJob*>(ctx->d_bounce_jobs), ctx->d_bounce_ctr);
-        VT_CUDA(ctx, cudaGetLastError());
-    }
     const int flat = ctx->tuning.bounce_walk == 1 ? 1 : 0;
     const int refill = ctx->tuning.bounce_refill > 0 ? ctx->tuning.bounce_refill : kRefill;
     if (ctx->bounce_blocks[flat] == 0) {

@@ -21,29 +21,14 @@ struct BounceJob {
     float o[3];
     float d[3];
     unsigned pixel;
-    unsigned tag;  // the frame number in per-thread slots (FrameParams::bounce_tag), else unused
+    unsigned pad;
 };
 static_assert(sizeof(BounceJob) == 32, "bounce job layout");
 
 // Appends one bounce ray; called by the lanes of a warp that have one, with
-// the warp possibly diverged (one atomic per converged group).  With a frame
-// tag the ray goes to the calling thread's own slot instead (its index in
-// the launch grid, so that slot order is image-tile order), tagged.
+// the warp possibly diverged (one atomic per converged group).
 __device__ __forceinline__ void append_bounce(const FrameParams& f, const float o[3], const float d[3],
                                               unsigned pixel) {
-    if (f.bounce_tag) {
-        const size_t slot = ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
-        BounceJob* j = reinterpret_cast<BounceJob*>(f.bounce_jobs) + slot;
-        j->o[0] = o[0];
-        j->o[1] = o[1];
-        j->o[2] = o[2];
-        j->d[0] = d[0];
-        j->d[1] = d[1];
-        j->d[2] = d[2];
-        j->pixel = pixel;
-        j->tag = f.bounce_tag;
-        return;
-    }
     const unsigned act = __activemask();
     const unsigned lane = threadIdx.x & 31u;
     const int leader = __ffs(act) - 1;
@@ -59,6 +44,98 @@ __device__ __forceinline__ void append_bounce(const FrameParams& f, const float 
     j->d[1] = d[1];
     j->d[2] = d[2];
     j->pixel = pixel;
+}
+
+// ---------------------------------------------------------------------------
+// Direction-binned deferral (tuning bounce_sort).  Consecutive queue entries
+// then start close together and head the same way, so that the lanes of a
+// warp in the trace kernel walk similar paths: every thread of a 256-thread
+// frame-kernel block (one 16 x 16-pixel tile) stages its bounce ray in the
+// block's shared memory, and at the block's end the block sorts its rays by
+// direction class (the cube-map face of the direction and a 4 x 4 cell on
+// it, 96 classes) and appends them with one atomic.
+constexpr int kStageThreads = 256;  // the frame kernel's block
+constexpr unsigned kBins = 96;
+constexpr unsigned char kNoBin = 0xFFu;
+
+struct BounceStage {
+    BounceJob job[kStageThreads];
+    unsigned char bin[kStageThreads];
+    unsigned hist[kBins];
+    unsigned base;
+};
+
+__device__ __forceinline__ BounceStage& bounce_stage() {
+    __shared__ BounceStage s;
+    return s;
+}
+
+__device__ __forceinline__ unsigned direction_bin(const float d[3]) {
+    const float ax = fabsf(d[0]), ay = fabsf(d[1]), az = fabsf(d[2]);
+    float m = ax, u = d[1], v = d[2], s = d[0];
+    unsigned face = 0;
+    if (ay > m && ay >= az) {
+        m = ay; u = d[0]; v = d[2]; s = d[1]; face = 2;
+    } else if (az > m && az > ay) {
+        m = az; u = d[0]; v = d[1]; s = d[2]; face = 4;
+    }
+    if (s < 0.0f) face += 1;
+    const float iu = (u / m + 1.0f) * 2.0f, iv = (v / m + 1.0f) * 2.0f;   // [0, 4]
+    const unsigned cu = iu >= 3.0f ? 3u : (iu >= 2.0f ? 2u : (iu >= 1.0f ? 1u : 0u));
+    const unsigned cv = iv >= 3.0f ? 3u : (iv >= 2.0f ? 2u : (iv >= 1.0f ? 1u : 0u));
+    return face * 16u + cu * 4u + cv;
+}
+
+// Every thread of the block, before any stage_bounce.
+__device__ __forceinline__ void stage_begin() { bounce_stage().bin[threadIdx.x] = kNoBin; }
+
+__device__ __forceinline__ void stage_bounce(const float o[3], const float d[3], unsigned pixel) {
+    BounceStage& st = bounce_stage();
+    BounceJob& j = st.job[threadIdx.x];
+    j.o[0] = o[0];
+    j.o[1] = o[1];
+    j.o[2] = o[2];
+    j.d[0] = d[0];
+    j.d[1] = d[1];
+    j.d[2] = d[2];
+    j.pixel = pixel;
+    st.bin[threadIdx.x] = (unsigned char)direction_bin(d);
+}
+
+// Every thread of the block, at its end: sorts the staged rays by class and
+// appends them to the queue (one atomic per block).
+__device__ __forceinline__ void stage_flush(const FrameParams& f) {
+    BounceStage& st = bounce_stage();
+    const unsigned t = threadIdx.x, lane = t & 31u;
+    if (t < kBins) st.hist[t] = 0u;
+    __syncthreads();
+    const unsigned b = st.bin[t];
+    // rank within the class: one shared atomic per class and warp
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+    const int leader = __ffs(peers) - 1;
+    unsigned wb = 0;
+    if ((int)lane == leader && b != kNoBin) wb = atomicAdd(&st.hist[b], (unsigned)__popc(peers));
+    wb = __shfl_sync(0xFFFFFFFFu, wb, leader);
+    const unsigned rank = wb + (unsigned)__popc(peers & ((1u << lane) - 1u));
+    __syncthreads();
+    if (t < 32) {
+        // exclusive scan of the class counts, 3 per lane
+        const unsigned a = st.hist[3 * lane], c1 = st.hist[3 * lane + 1], c2 = st.hist[3 * lane + 2];
+        unsigned incl = a + c1 + c2;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if ((int)lane >= o) incl += v;
+        }
+        const unsigned excl = incl - (a + c1 + c2);
+        st.hist[3 * lane] = excl;
+        st.hist[3 * lane + 1] = excl + a;
+        st.hist[3 * lane + 2] = excl + a + c1;
+        const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        if (lane == 31) st.base = total ? atomicAdd(f.bounce_count, total) : 0u;
+    }
+    __syncthreads();
+    if (b != kNoBin) reinterpret_cast<BounceJob*>(f.bounce_jobs)[st.base + st.hist[b] + rank] = st.job[t];
 }
 
 }  // namespace vt

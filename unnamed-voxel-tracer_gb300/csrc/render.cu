@@ -45,8 +45,9 @@ struct BlockTile {
 };
 
 // SHARE: the lanes of a warp that look up the same brick word share one load
-// (Walker::brick_word).
-template <bool STATS, bool CHECKED, bool SMEM, int TW, bool OCC, bool SHARE = false>
+// (Walker::brick_word).  BIN: deferred bounce rays are appended per block,
+// sorted by direction (stage_flush).
+template <bool STATS, bool CHECKED, bool SMEM, int TW, bool OCC, bool SHARE = false, bool BIN = false>
 __global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldView w, FrameParams f, uint4* __restrict__ out,
                                                                unsigned* status, unsigned long long* counters) {
     // shared copy of the coarse bits for the model traversal (STATS or
@@ -72,6 +73,7 @@ __global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldVi
     if (SMEM)
         for (unsigned i = threadIdx.x; i < w.ncoarse; i += blockDim.x) s_coarse[i] = __ldg(w.coarse + i);
     if (SMEM || !table) __syncthreads();
+    if (BIN) stage_begin();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int lx = (warp % BT::kWarpsX) * TW + (lane % TW), ly = (warp / BT::kWarpsX) * (32 / TW) + (lane / TW);
     const int px = x0 + lx, py = y0 + ly;
@@ -92,10 +94,11 @@ __global__ void __launch_bounds__(kBlock, OCC ? kOccBlocks : 1) k_render(WorldVi
         }
         uint4 rec;
         if (SMEM) rec = render_pixel<STATS, CHECKED>(w, CoarseShared{s_coarse}, w.cdist, f, px, py, uv, status, pc);
-        else rec = render_pixel<STATS, CHECKED, CoarseGlobal, SHARE>(w, CoarseGlobal{w.coarse}, w.cdist, f, px, py, uv,
-                                                                     status, pc);
+        else rec = render_pixel<STATS, CHECKED, CoarseGlobal, SHARE, BIN>(w, CoarseGlobal{w.coarse}, w.cdist, f, px,
+                                                                          py, uv, status, pc);
         out[(size_t)py * f.width + px] = rec;
     }
+    if (BIN) stage_flush(f);
     flush_counters<STATS>(pc, counters);
 }
 
@@ -301,7 +304,6 @@ FrameParams make_frame(const vt_camera* cam, const vt_params* p) {
     f.row_end = cam->height;
     f.bounce_jobs = nullptr;
     f.bounce_count = nullptr;
-    f.bounce_tag = 0;
     f.screen = nullptr;
     f.max_steps = p->max_steps;
     f.shadow_max_steps = p->shadow_max_steps;
@@ -451,29 +453,15 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         if (s) return s;
     }
     const bool defer = allow_defer && (p->rays & VT_RAYS_BOUNCE) && !stats && !checked;
-    size_t nslots = 0;
+    // the direction-sorted append exists for the default 8 x 4 capped tile kernel
+    const bool binned = defer && tu.bounce_sort && tu.warp_tile_w == 8 && tu.occupancy && !tu.share_bricks;
     if (defer) {
         vt_status s = bounce_buffers(ctx, (size_t)cam->width * (size_t)cam->height);
         if (s) return s;
-        if (tu.bounce_sort) {
-            // one slot per thread of the launch below
-            const int tw = tu.warp_tile_w == 4 ? 4 : (tu.warp_tile_w == 16 ? 16 : (tu.warp_tile_w == 32 ? 32 : 8));
-            const int bw = tw == 4 ? BlockTile<4>::kW : (tw == 16 ? BlockTile<16>::kW : (tw == 32 ? BlockTile<32>::kW : BlockTile<8>::kW));
-            const int bh = tw == 4 ? BlockTile<4>::kH : (tw == 16 ? BlockTile<16>::kH : (tw == 32 ? BlockTile<32>::kH : BlockTile<8>::kH));
-            nslots = (size_t)((cam->width + bw - 1) / bw) * (size_t)((rows + bh - 1) / bh) * kBlock;
-            s = bounce_slots(ctx, nslots);
-            if (s) return s;
-        }
         VT_CUDA(ctx, cudaStreamWaitEvent(stream, ctx->ev_bounce, 0));
         VT_CUDA(ctx, cudaMemsetAsync(ctx->d_bounce_ctr, 0, 2 * sizeof(unsigned), stream));
+        f.bounce_jobs = ctx->d_bounce_jobs;
         f.bounce_count = ctx->d_bounce_ctr;
-        if (nslots) {
-            if (++ctx->bounce_tag == 0) ctx->bounce_tag = 1;  // (0 means "no tag")
-            f.bounce_jobs = ctx->d_bounce_slots;
-            f.bounce_tag = ctx->bounce_tag;
-        } else {
-            f.bounce_jobs = ctx->d_bounce_jobs;
-        }
     }
     cudaError_t le = cudaSuccess;
 #define VT_LAUNCH_X(S, C, M, TW, O, SH)                                                                         \
@@ -499,7 +487,11 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
         if (tu.occupancy) { VT_LAUNCH(false, false, false, 32, true); }
         else { VT_LAUNCH(false, false, false, 32, false); }
     } else {
-        if (tu.occupancy && tu.share_bricks) { VT_LAUNCH_X(false, false, false, 8, true, true); }
+        if (binned) { le = launch_kernel(k_render<false, false, false, 8, true, false, true>,
+                                         dim3((cam->width + BlockTile<8>::kW - 1) / BlockTile<8>::kW,
+                                              (rows + BlockTile<8>::kH - 1) / BlockTile<8>::kH),
+                                         dim3(kBlock), sm, stream, win, w, f, d_out, ctx->d_status, ctx->d_counters); }
+        else if (tu.occupancy && tu.share_bricks) { VT_LAUNCH_X(false, false, false, 8, true, true); }
         else if (tu.occupancy) { VT_LAUNCH(false, false, false, 8, true); }
         else { VT_LAUNCH(false, false, false, 8, false); }
     }
@@ -508,7 +500,7 @@ vt_status launch_render(vt_ctx* ctx, const vt_world* world, const vt_camera* cam
 #undef VT_LAUNCH_X
     VT_CUDA(ctx, le);
     if (stats || checked) return note_status_writer(ctx, stream);  // the model walk checks its indexes
-    if (defer) return launch_bounce(ctx, world, f, d_out, stream, nslots);
+    if (defer) return launch_bounce(ctx, world, f, d_out, stream);
     return VT_OK;
 }
 

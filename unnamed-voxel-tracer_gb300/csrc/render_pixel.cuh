@@ -30,7 +30,9 @@ __device__ __forceinline__ bool trace_any(const WorldView& w, const Coarse& coar
 
 // uv: the pixel's screen coordinates (pixel_uv(f, px, py); the frame kernel
 // reads them from the frame's screen table or its per-block tables).
-template <bool STATS, bool CHECKED, class Coarse, bool SHARE = false>
+// BIN: a deferred bounce ray is staged in the block's shared memory for the
+// block's direction-sorted append (stage_flush) instead of appended at once.
+template <bool STATS, bool CHECKED, class Coarse, bool SHARE = false, bool BIN = false>
 __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& coarse, const unsigned char* cd,
                                               const FrameParams& f, int px, int py, const PixelUV& uv,
                                               unsigned* status, PixelCounters& pc) {
@@ -94,7 +96,8 @@ __device__ __forceinline__ uint4 render_pixel(const WorldView& w, const Coarse& 
         }
         if (deferred) {
             // traced and shaded by the bounce kernels (bounce.cu)
-            append_bounce(f, so, bdir, (unsigned)py * (unsigned)f.width + (unsigned)px);
+            if (BIN) stage_bounce(so, bdir, (unsigned)py * (unsigned)f.width + (unsigned)px);
+            else append_bounce(f, so, bdir, (unsigned)py * (unsigned)f.width + (unsigned)px);
         } else if (f.rays & VT_RAYS_BOUNCE) {
             PRay rb;
             pray_init(rb, so, bdir);

@@ -37,8 +37,6 @@ struct FrameParams {
     int row0, row_end;  // rows [row0, row_end) of the image this launch renders
     void* bounce_jobs;       // non-null: bounce rays are queued here (BounceJob), not traced inline
     unsigned* bounce_count;  // the queue's length
-    unsigned bounce_tag;     // non-zero: each thread writes its bounce ray to its own slot of bounce_jobs
-                             // (its index in the launch grid), tagged with this frame number
     const float4* screen;    // the frame's screen table (ScreenTable), or null: computed per block
 };
 

@@ -121,12 +121,6 @@ struct vt_ctx {
     unsigned char* d_bounce_open = nullptr;
     unsigned* d_bounce_ctr = nullptr;  // {queued, taken}
     size_t bounce_capacity = 0;
-    // direction-binned bounce pass (tuning bounce_sort): per-thread slots of
-    // the frame kernel, the frame number that tags this frame's slots
-    void* d_bounce_slots = nullptr;
-    size_t bounce_slot_capacity = 0;
-    unsigned bounce_tag = 0;
-    bool bin_smem_set = false;
     cudaEvent_t ev_bounce = nullptr;   // the last deferred frame is done with the queue
     // screen tables of the frame sizes rendered so far (see screen_table)
     vt::ScreenTable screen[vt::kScreenTables];
@@ -250,16 +244,9 @@ vt_status l2_policy(vt_ctx* ctx, const vt_world* world, cudaAccessPolicyWindow* 
 // The deferred bounce pass: queue buffers for `pixels` rays, and the trace +
 // shade kernels for a frame whose render kernel queued them.
 vt_status bounce_buffers(vt_ctx* ctx, size_t pixels);
-// The per-thread slots of a direction-binned bounce pass (zeroed when made:
-// a slot holds a ray of this frame only when it carries this frame's tag).
-vt_status bounce_slots(vt_ctx* ctx, size_t slots);
 // The context's band streams and events (created on first use).
 vt_status band_streams(vt_ctx* ctx);
-// nslots: the frame kernel's threads when its bounce rays went to per-thread
-// slots (f.bounce_tag != 0), which a binning kernel first compacts into the
-// queue, grouped by direction within each run of slots.
-vt_status launch_bounce(vt_ctx* ctx, const vt_world* world, const FrameParams& f, uint4* d_out, cudaStream_t st,
-                        size_t nslots = 0);
+vt_status launch_bounce(vt_ctx* ctx, const vt_world* world, const FrameParams& f, uint4* d_out, cudaStream_t st);
 }  // namespace vt
 
 #define VT_CUDA(ctx, call)                                                      \
