@@ -347,6 +347,17 @@ struct Walker {
     // Sets up the walk; false if the ray misses the grid or may take no step.
     __device__ __forceinline__ bool start(const WorldView& w, const float o[3], const float d[3], int steps) {
         pray_init(r, o, d);
+        return start_ray(w, steps);
+    }
+
+    // The same for a ray already set up in r (its reciprocals computed once,
+    // by the caller: pray_init, or pray_init_dir with a frame's shared ones).
+    __device__ __forceinline__ bool start_ray(const WorldView& w, const PRay& ray, int steps) {
+        r = ray;
+        return start_ray(w, steps);
+    }
+
+    __device__ __forceinline__ bool start_ray(const WorldView& w, int steps) {
         max_steps = steps;
         if (!pray_start(r, w.dims, c, t, axis)) return false;
         if (steps <= 0) return false;
@@ -603,7 +614,7 @@ template <bool MAT, bool RUN = true, bool NEAR = false, bool SHARE = false>
 __device__ __forceinline__ bool trace_fast(const WorldView& w, const unsigned char* cdist, const PRay& r,
                                            int max_steps, TraceHit& h) {
     Walker wk;
-    if (!wk.start(w, r.o, r.d, max_steps)) return false;
+    if (!wk.start_ray(w, r, max_steps)) return false;
     int s;
     while ((s = wk.step<MAT, RUN, NEAR, SHARE>(w, cdist, h)) == Walker::kMore) {
     }
