@@ -380,6 +380,12 @@ vt_status vt_batch_launch(vt_batch* batch, vt_stream stream);
 vt_status vt_batch_destroy(vt_batch* batch);
 /* Pixels (= primary rays), jobs and 16x16 work units of one launch. */
 vt_status vt_batch_info(const vt_batch* batch, uint64_t* pixels, int32_t* jobs, uint32_t* units);
+/* Times the batch in each launch shape (VT_KERNEL_TILE: one launch per world;
+ * VT_KERNEL_PER_JOB: one launch per job; VT_KERNEL_QUEUE: one persistent
+ * kernel), reps graph launches each on the context's stream (synchronous),
+ * and keeps the fastest for this batch's later launches.  Every shape gives
+ * identical records.  No counterpart in the reference. */
+vt_status vt_batch_autotune(vt_batch* batch, int32_t reps, int32_t* best_shape, float* best_ms);
 
 /* ------------------------------------------------------- shading adjoint
  * No counterpart in the reference (its shading is fixed-function,

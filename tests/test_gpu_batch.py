@@ -122,3 +122,35 @@ def test_batch_many_chunks(vt, ctx, checked):
             buf.free()
         for w in worlds:
             w.close()
+
+
+def test_batch_autotune_keeps_identical_records(vt, ctx):
+    """vt_batch_autotune times the three launch shapes, keeps the fastest,
+    and the batch launched afterwards still equals the per-job renders."""
+    params = vt.default_params(rays=vt.RAYS_PRIMARY | vt.RAYS_SHADOW, sun_dir=vt.gen_sun(51))
+    worlds, jobs = [], []
+    try:
+        for s, edge in enumerate((48, 96, 130)):
+            d = vt.gen_desc((edge, edge, edge), scale=edge / 128.0, seed=950 + s)
+            w = vt.World(ctx, (edge, edge, edge))
+            w.upload_dense(vt.gen_world(d))
+            worlds.append(w)
+            for c, (W, H) in enumerate([(120, 90), (64, 33)]):
+                cam = vt.gen_camera(d, c, W, H)
+                jobs.append((w, cam, ctx.alloc(W * H * 16)))
+        batch = vt.Batch(ctx, jobs, params)
+        shape, ms = batch.autotune(reps=2)
+        assert shape in (vt.KERNEL_TILE, vt.KERNEL_QUEUE, vt.KERNEL_PER_JOB) and ms > 0
+        for _, _, buf in jobs:
+            buf.zero()
+        batch.launch()
+        ctx.sync()
+        for w, cam, buf in jobs:
+            got = buf.download(np.zeros(cam.width * cam.height, vt.HIT_DTYPE))
+            assert np.array_equal(got, vt.render_host(ctx, w, cam, params))
+        batch.close()
+    finally:
+        for _, _, buf in jobs:
+            buf.free()
+        for w in worlds:
+            w.close()

@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(kBatchBlock, 3) k_render_batch(const JobDesc* 
 
 struct vt_batch {
     vt_ctx* ctx = nullptr;
+    int shape = -1;  // VT_KERNEL_* of the captured graph; -1: the context's tuning at the first launch
     std::vector<const vt_world*> worlds;
     std::vector<vt_job> jobs;
     vt_params params;
@@ -293,7 +294,8 @@ vt_status vt_batch_launch(vt_batch* b, vt_stream stream) {
     }
     const bool checked = (b->params.flags & VT_FLAG_CHECKED) != 0;
     if (!b->exec) {
-        const int shape = ctx->tuning.kernel;
+        if (b->shape < 0) b->shape = ctx->tuning.kernel;
+        const int shape = b->shape;
         if (shape == VT_KERNEL_TILE) {
             vt_status s = build_chunks(b);   // before the capture: may make screen tables
             if (s) return s;
@@ -366,6 +368,53 @@ vt_status vt_batch_destroy(vt_batch* b) {
     vt::dev_free(b->d_jobs);
     vt::dev_free(b->d_counter);
     delete b;
+    return VT_OK;
+}
+
+vt_status vt_batch_autotune(vt_batch* b, int32_t reps, int32_t* best_shape, float* best_ms) {
+    if (!b) return VT_ERR_ARG;
+    vt_ctx* ctx = b->ctx;
+    if (reps < 1 || reps > 10000) return fail(ctx, VT_ERR_ARG, "reps must be in [1, 10000]");
+    cudaEvent_t e0, e1;
+    VT_CUDA(ctx, cudaEventCreate(&e0));
+    VT_CUDA(ctx, cudaEventCreate(&e1));
+    vt_status s = VT_OK;
+    int win = -1;
+    float win_ms = 0.0f;
+    for (int shape : {VT_KERNEL_TILE, VT_KERNEL_PER_JOB, VT_KERNEL_QUEUE}) {
+        // drop the captured graph; the next launch captures this shape
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
+        b->shape = shape;
+        for (int i = 0; i < 2 && !s; ++i) s = vt_batch_launch(b, ctx->stream);
+        if (!s) s = check_cuda(ctx, cudaEventRecord(e0, ctx->stream), "cudaEventRecord");
+        for (int i = 0; i < reps && !s; ++i) s = vt_batch_launch(b, ctx->stream);
+        if (!s) s = check_cuda(ctx, cudaEventRecord(e1, ctx->stream), "cudaEventRecord");
+        if (!s) s = check_cuda(ctx, cudaEventSynchronize(e1), "cudaEventSynchronize");
+        float ms = 0.0f;
+        if (!s) s = check_cuda(ctx, cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        if (s) break;
+        ms /= (float)reps;
+        if (win < 0 || ms < win_ms) {
+            win = shape;
+            win_ms = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    if (s) {
+        b->shape = -1;
+        return s;
+    }
+    b->shape = win;  // captured at the next launch
+    if (best_shape) *best_shape = win;
+    if (best_ms) *best_ms = win_ms;
     return VT_OK;
 }
 

@@ -162,6 +162,7 @@ _SIGNATURES = {
     "vt_batch_launch": (_S, [_P, _P]),
     "vt_batch_destroy": (_S, [_P]),
     "vt_batch_info": (_S, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_int32), C.POINTER(C.c_uint32)]),
+    "vt_batch_autotune": (_S, [_P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
     "vt_probe_read_bandwidth": (_S, [_P, C.c_uint64, C.c_int32, C.POINTER(C.c_float)]),
     "vt_set_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
     "vt_get_tuning": (_S, [_P, C.POINTER(Tuning_t)]),
@@ -613,6 +614,12 @@ class Batch:
 
     def launch(self, stream=None) -> None:
         self.ctx.check(self.ctx.lib.vt_batch_launch(self.handle, stream))
+
+    def autotune(self, reps: int = 3) -> tuple[int, float]:
+        """Times each launch shape and keeps the fastest: (shape, ms)."""
+        shape, ms = C.c_int32(), C.c_float()
+        self.ctx.check(self.ctx.lib.vt_batch_autotune(self.handle, reps, C.byref(shape), C.byref(ms)))
+        return shape.value, ms.value
 
     def info(self) -> dict:
         px, nj, nu = C.c_uint64(), C.c_int32(), C.c_uint32()
