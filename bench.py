@@ -330,7 +330,7 @@ def measure_config1_frames(vt, ctx, torch, flush) -> dict:
     return {"workload": workload_config()["workload"], "ms_per_frame": sum(ms) / len(ms), "tuning": ctx.get_tuning()}
 
 
-def measure_config0(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py) -> dict:
+def measure_config0(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py, autotune: bool = True) -> dict:
     """128^3 terrain, 640x360 primary rays (max 512 steps): the small plain
     scene that the CPU oracle also renders whole."""
     desc, cams, params = scenes.config0()
@@ -341,7 +341,11 @@ def measure_config0(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py) -
     out = ctx.alloc(cam.width * cam.height * 16)
     sh = torch.cuda.current_stream().cuda_stream
     st = vt.render_stats(ctx, w, cam, params, sh)
-    tuning, _ = ctx.autotune(w, cam, params, reps=20)   # the library's own choice for this frame
+    before = ctx.get_tuning()
+    if autotune:
+        tuning, _ = ctx.autotune(w, cam, params, reps=20)   # the library's own choice for this frame
+    else:
+        tuning = before
 
     def frame():
         ctx.check(ctx.lib.vt_render(ctx.handle, w.handle, C.byref(cam), C.byref(params), out.ptr, sh))
@@ -349,7 +353,7 @@ def measure_config0(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py) -
     for _ in range(3):
         frame()
     ms = _timed_flushed(torch, frame, 50, flush)
-    ctx.set_tuning()
+    ctx.set_tuning(**before)
     w.close()
     out.free()
     rays = st["primary_rays"]
@@ -360,13 +364,14 @@ def measure_config0(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py) -
     dt = time.perf_counter() - t0
     return {"workload": "128^3 terrain (fbm, water), 640x360 primary rays, max 512 steps",
             "grays_per_s": rays / (ms * 1e-3) / 1e9, "ms_per_frame": ms, "rays_per_frame": rays,
-            "l2": "flushed before each frame", "tuning": {"by": "vt_autotune on this frame", **tuning},
+            "l2": "flushed before each frame",
+            "tuning": {"by": "vt_autotune on this frame" if autotune else "given", **tuning},
             "roofline": roofline(ray_bytes(st), ms * 1e-3, peak, peak_kind, RAY_BYTES),
             "cpu_baseline": {"value": cst["primary_rays"] / dt / 1e9, "unit": "Grays/s", "cores": threads,
                              "kind": "port", "sample": f"the whole frame ({cst['primary_rays']} rays, {dt:.2f} s)"}}
 
 
-def measure_config2(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py) -> dict:
+def measure_config2(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py, autotune: bool = True) -> dict:
     """2048x256x2048 world with caves (1 GiB of materials, 128 MiB of mask
     words), 3840x2160 primary + shadow + bounce rays."""
     desc, cams, params = scenes.config2()
@@ -376,14 +381,18 @@ def measure_config2(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py) -
     sh = torch.cuda.current_stream().cuda_stream
     stats = [vt.render_stats(ctx, w, c, params, sh) for c in cams]
     rays = [s["primary_rays"] + s["shadow_rays"] + s["bounce_rays"] for s in stats]
-    tuning, _ = ctx.autotune(w, cams[0], params, reps=2)   # the library's own choice for this frame size
+    before = ctx.get_tuning()
+    if autotune:
+        tuning, _ = ctx.autotune(w, cams[0], params, reps=2)   # the library's own choice for this frame size
+    else:
+        tuning = before
     ms = []
     for c in cams:
         def frame():
             ctx.check(ctx.lib.vt_render(ctx.handle, w.handle, C.byref(c), C.byref(params), out.ptr, sh))
         frame()
         ms.append(_timed_flushed(torch, frame, 3, flush))
-    ctx.set_tuning()
+    ctx.set_tuning(**before)
     mats = w.download_dense()
     w.close()
     out.free()
@@ -395,7 +404,7 @@ def measure_config2(vt, scenes, ctx, torch, flush, peak, peak_kind, oracle_py) -
     return {"workload": "2048x256x2048 world + caves, 3840x2160, primary + shadow + 1 cosine bounce per hit",
             "grays_per_s": sum(rays) / t / 1e9, "ms_per_frame": sum(ms) / len(ms),
             "rays_per_frame": sum(rays) / len(rays), "l2": "flushed before each frame (the mask alone is 128 MiB)",
-            "tuning": {"by": "vt_autotune on camera 0's frame", **tuning},
+            "tuning": {"by": "vt_autotune on camera 0's frame" if autotune else "given", **tuning},
             "roofline": roofline(sum(ray_bytes(s) for s in stats) / len(stats), t / len(stats), peak, peak_kind,
                                  RAY_BYTES + ", bounce rays included"),
             "cpu_baseline": {"value": r / 1e9, "unit": "Grays/s", "cores": threads, "kind": "port",
@@ -829,9 +838,10 @@ def main() -> None:
             ctx.set_tuning(**{k: int(v) for k, v in (kv.split("=") for kv in args.tuning.split(","))})
         peak, kind = read_peaks()
         flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-        fn = {"config0": lambda: measure_config0(vt, scenes, ctx, torch, flush, peak, kind, oracle_py),
+        fixed = bool(args.tuning)   # a given tuning is profiled as given, not autotuned
+        fn = {"config0": lambda: measure_config0(vt, scenes, ctx, torch, flush, peak, kind, oracle_py, not fixed),
               "config1": lambda: measure_config1_frames(vt, ctx, torch, flush),
-              "config2": lambda: measure_config2(vt, scenes, ctx, torch, flush, peak, kind, oracle_py),
+              "config2": lambda: measure_config2(vt, scenes, ctx, torch, flush, peak, kind, oracle_py, not fixed),
               "config3": lambda: measure_config3(vt, scenes, ctx, torch, peak, kind, oracle_py),
               "config4": lambda: measure_config4(vt, scenes, ctx, torch, peak, kind, oracle_py)}[args.only]
         print(json.dumps({"only": args.only, **fn()}), flush=True)
