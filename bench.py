@@ -823,7 +823,8 @@ def main() -> None:
     ap.add_argument("--only", choices=["config0", "config1", "config2", "config3", "config4"],
                     help="run just one workload and print its result (for profiling)")
     ap.add_argument("--tuning", default="",
-                    help="with --only: vt_tuning fields for the context, e.g. share_bricks=1,l2_persist=1")
+                    help="with --only: vt_tuning fields for the context, e.g. share_bricks=1,l2_persist=1 "
+                         "(--only runs never autotune)")
     args = ap.parse_args()
     if args.only:
         import torch
@@ -838,7 +839,7 @@ def main() -> None:
             ctx.set_tuning(**{k: int(v) for k, v in (kv.split("=") for kv in args.tuning.split(","))})
         peak, kind = read_peaks()
         flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-        fixed = bool(args.tuning)   # a given tuning is profiled as given, not autotuned
+        fixed = True   # profiling: the given tuning (or the default) as it is, launch order fixed
         fn = {"config0": lambda: measure_config0(vt, scenes, ctx, torch, flush, peak, kind, oracle_py, not fixed),
               "config1": lambda: measure_config1_frames(vt, ctx, torch, flush),
               "config2": lambda: measure_config2(vt, scenes, ctx, torch, flush, peak, kind, oracle_py, not fixed),
