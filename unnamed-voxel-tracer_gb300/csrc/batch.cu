@@ -3,10 +3,11 @@
 // A batch (jobs of a world, a camera and an output buffer each) is captured
 // once into a CUDA graph and replayed with one cudaGraphLaunch.  Three shapes:
 //
-//   tile (default)  the consecutive jobs of each world (up to kLaunchJobs)
-//                   are ONE launch of k_render_jobs whose grid covers every
-//                   16 x 16-pixel tile of all of them, on kBatchChains
-//                   concurrent chains of the graph.  The launch's job table
+//   tile (default)  the consecutive jobs of each world (up to kLaunchJobs
+//                   jobs and about 4 Mpixels) are ONE launch of k_render_jobs
+//                   whose grid covers every 16 x 16-pixel tile of all of
+//                   them, on kBatchChains concurrent chains of the graph
+//                   (longest launch first, on the least loaded chain).  The launch's job table
 //                   (the world, the shared frame settings, each job's camera,
 //                   output and first tile) is the kernel's parameter block
 //                   itself (__grid_constant__, < 32 KB): a block finds its
@@ -17,7 +18,8 @@
 //                   tail.
 //   per job         (VT_KERNEL_PER_JOB) one production k_render launch per
 //                   job, spread over kBatchChains concurrent chains of the
-//                   graph, so that one job's tail overlaps the next jobs.
+//                   graph the same way, so that one job's tail overlaps the
+//                   next jobs.
 //   queue           (VT_KERNEL_QUEUE) one persistent launch: a warp takes
 //                   16 x 16 pixel units from a device counter, finds its job
 //                   by binary search over the jobs' first-unit numbers and
@@ -44,6 +46,9 @@ constexpr int kBatchChains = 8;  // 4, 8, 16 and 32 chains measured within 1% on
 
 // ---------------------------------------------------------------- tile shape
 constexpr int kLaunchJobs = 256;
+// A launch holds at most this many 16 x 16 blocks (about 4 Mpixels) unless
+// one camera alone is larger: finer launches balance the graph's chains.
+constexpr unsigned kLaunchBlocks = 16384;
 
 // Per-job camera fields of a tile-shape launch.
 struct JobCam {
@@ -189,8 +194,9 @@ using namespace vt;
 namespace {
 
 // Cuts the jobs into launch chunks: consecutive jobs of one world, at most
-// kLaunchJobs each.  The frames get the context's screen tables (made here if
-// missing: an allocation and a synchronisation).
+// kLaunchJobs jobs and (unless one job alone is larger) kLaunchBlocks blocks
+// each.  The frames get the context's screen tables (made here if missing: an
+// allocation and a synchronisation).
 vt_status build_chunks(vt_batch* b) {
     vt_ctx* ctx = b->ctx;
     b->chunks.clear();
@@ -200,7 +206,10 @@ vt_status build_chunks(vt_batch* b) {
         FrameParams f = make_frame(&j.camera, &b->params);
         vt_status s = screen_table(ctx, f, ctx->stream, true, &f.screen);
         if (s) return s;
-        if (!c || c->njobs == kLaunchJobs || c->w.mask != j.world->d_mask) {
+        const unsigned long long job_blocks = (unsigned long long)((j.camera.width + kUnit - 1) / kUnit) *
+                                              (unsigned long long)((j.camera.height + kUnit - 1) / kUnit);
+        if (!c || c->njobs == kLaunchJobs || c->w.mask != j.world->d_mask ||
+            (c->njobs > 0 && (unsigned long long)c->first_block[c->njobs] + job_blocks > kLaunchBlocks)) {
             b->chunks.emplace_back();
             c = &b->chunks.back();
             std::memset(c, 0, sizeof(*c));
@@ -224,6 +233,26 @@ vt_status build_chunks(vt_batch* b) {
         c->first_block[n + 1] = (unsigned)end;
     }
     return VT_OK;
+}
+
+// The graph's launches over kBatchChains chains, longest first, each on the
+// chain with the least work so far (weights: blocks or pixels): the chains
+// end close together.  Returns (launch index, chain) in issue order.
+std::vector<std::pair<size_t, int>> chain_plan(const std::vector<double>& weight) {
+    std::vector<size_t> order(weight.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return weight[a] > weight[b]; });
+    double load[kBatchChains] = {};
+    std::vector<std::pair<size_t, int>> plan;
+    plan.reserve(order.size());
+    for (size_t i : order) {
+        int best = 0;
+        for (int k = 1; k < kBatchChains; ++k)
+            if (load[k] < load[best]) best = k;
+        load[best] += weight[i];
+        plan.emplace_back(i, best);
+    }
+    return plan;
 }
 
 }  // namespace
@@ -317,23 +346,30 @@ vt_status vt_batch_launch(vt_batch* b, vt_stream stream) {
                 cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), cap);
                 k_render_batch<<<b->blocks, kBatchBlock, 0, cap>>>(b->d_jobs, b->njobs, b->total_units, b->d_counter);
             } else {
-                // fork chains off the capture stream, launches round robin, join
+                // fork chains off the capture stream, launches longest first on
+                // the least loaded chain (chain_plan), join
                 cudaEventRecord(fork, cap);
                 for (int k = 0; k < kBatchChains; ++k) cudaStreamWaitEvent(chain[k], fork, 0);
                 if (shape == VT_KERNEL_TILE) {
-                    for (size_t c = 0; c < b->chunks.size(); ++c) {
-                        const JobChunk& ch = b->chunks[c];
+                    std::vector<double> wt(b->chunks.size());
+                    for (size_t c = 0; c < wt.size(); ++c) wt[c] = b->chunks[c].first_block[b->chunks[c].njobs];
+                    for (const auto& pc : chain_plan(wt)) {
+                        const JobChunk& ch = b->chunks[pc.first];
                         const unsigned blocks = ch.first_block[ch.njobs];
                         if (checked)
-                            k_render_jobs<true><<<blocks, kBatchBlock, 0, chain[c % kBatchChains]>>>(ch, ctx->d_status);
+                            k_render_jobs<true><<<blocks, kBatchBlock, 0, chain[pc.second]>>>(ch, ctx->d_status);
                         else
-                            k_render_jobs<false><<<blocks, kBatchBlock, 0, chain[c % kBatchChains]>>>(ch, nullptr);
+                            k_render_jobs<false><<<blocks, kBatchBlock, 0, chain[pc.second]>>>(ch, nullptr);
                     }
                 } else {
-                    for (size_t j = 0; j < b->jobs.size() && !s; ++j) {
-                        const vt_job& jb = b->jobs[j];
+                    std::vector<double> wt(b->jobs.size());
+                    for (size_t j = 0; j < wt.size(); ++j)
+                        wt[j] = (double)b->jobs[j].camera.width * (double)b->jobs[j].camera.height;
+                    for (const auto& pc : chain_plan(wt)) {
+                        if (s) break;
+                        const vt_job& jb = b->jobs[pc.first];
                         s = launch_render(ctx, jb.world, &jb.camera, &b->params, reinterpret_cast<uint4*>(jb.d_out),
-                                          chain[j % kBatchChains], false);
+                                          chain[pc.second], false);
                     }
                 }
                 for (int k = 0; k < kBatchChains; ++k) {
