@@ -30,47 +30,84 @@ static inline unsigned atomicOr(unsigned* p, unsigned v) { unsigned o = *p; *p |
 
 #include "../../unnamed-voxel-tracer_gb300/csrc/trace_p.cuh"
 
-// Distance max(|dx|, wy*|dy|, |dz|) (capped at kDistCap + 1) from each cell of
-// a gx*gy*gz occupancy grid to the nearest occupied cell ahead in octant oct
-// (bit i set: d_i >= 0, else d_i <= 0).  Computed independently of the
-// library's separable passes: the smallest r whose box (r cells ahead in x
-// and z, r / wy in y) holds an occupied cell, counted with a summed-area
-// table.
-static std::vector<unsigned char> cheb(const std::vector<unsigned char>& occ, int gx, int gy, int gz, int wy,
-                                       int oct) {
-    const int cap = vt::kDistCap;
-    const size_t sx = gx + 1, sy = gy + 1;
-    std::vector<int> sat(sx * sy * (gz + 1), 0);
-    auto S = [&](int x, int y, int z) -> int& { return sat[(size_t)x + sx * ((size_t)y + sy * z)]; };
-    for (int z = 0; z < gz; ++z)
-        for (int y = 0; y < gy; ++y)
-            for (int x = 0; x < gx; ++x)
-                S(x + 1, y + 1, z + 1) = occ[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] + S(x, y + 1, z + 1) +
-                                         S(x + 1, y, z + 1) + S(x + 1, y + 1, z) - S(x, y, z + 1) - S(x, y + 1, z) -
-                                         S(x + 1, y, z) + S(x, y, z);
-    auto count = [&](int x0, int x1, int y0, int y1, int z0, int z1) {  // inclusive, clipped
+// Summed-area table of an occupancy grid: count(box) in O(1).
+struct Sat {
+    int gx, gy, gz;
+    std::vector<int> s;
+    template <class Occ>
+    Sat(int x_, int y_, int z_, Occ occ) : gx(x_), gy(y_), gz(z_), s((size_t)(x_ + 1) * (y_ + 1) * (z_ + 1), 0) {
+        for (int z = 0; z < gz; ++z)
+            for (int y = 0; y < gy; ++y)
+                for (int x = 0; x < gx; ++x)
+                    at(x + 1, y + 1, z + 1) = (occ(x, y, z) ? 1 : 0) + at(x, y + 1, z + 1) + at(x + 1, y, z + 1) +
+                                              at(x + 1, y + 1, z) - at(x, y, z + 1) - at(x, y + 1, z) -
+                                              at(x + 1, y, z) + at(x, y, z);
+    }
+    int& at(int x, int y, int z) { return s[(size_t)x + (size_t)(gx + 1) * ((size_t)y + (size_t)(gy + 1) * z)]; }
+    int count(int x0, int x1, int y0, int y1, int z0, int z1) {  // inclusive, clipped to the grid
         x0 = std::max(x0, 0); y0 = std::max(y0, 0); z0 = std::max(z0, 0);
         x1 = std::min(x1, gx - 1); y1 = std::min(y1, gy - 1); z1 = std::min(z1, gz - 1);
         if (x0 > x1 || y0 > y1 || z0 > z1) return 0;
-        return S(x1 + 1, y1 + 1, z1 + 1) - S(x0, y1 + 1, z1 + 1) - S(x1 + 1, y0, z1 + 1) - S(x1 + 1, y1 + 1, z0) +
-               S(x0, y0, z1 + 1) + S(x0, y1 + 1, z0) + S(x1 + 1, y0, z0) - S(x0, y0, z0);
-    };
+        return at(x1 + 1, y1 + 1, z1 + 1) - at(x0, y1 + 1, z1 + 1) - at(x1 + 1, y0, z1 + 1) - at(x1 + 1, y1 + 1, z0) +
+               at(x0, y0, z1 + 1) + at(x0, y1 + 1, z0) + at(x1 + 1, y0, z0) - at(x0, y0, z0);
+    }
+};
+
+// Chunk distances: max(|dx|, |dy|, |dz|) (capped at kDistCap + 1) from each
+// cell of a gx*gy*gz occupancy grid to the nearest occupied cell ahead in
+// octant oct (bit i set: d_i >= 0, else d_i <= 0).  Computed independently of
+// the library's separable passes: the smallest r whose box (r cells ahead)
+// holds an occupied cell, counted with a summed-area table.
+static std::vector<unsigned char> cheb(const std::vector<unsigned char>& occ, int gx, int gy, int gz, int oct) {
+    Sat sat(gx, gy, gz, [&](int x, int y, int z) { return occ[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] != 0; });
     std::vector<unsigned char> d((size_t)gx * gy * gz);
     for (int z = 0; z < gz; ++z)
         for (int y = 0; y < gy; ++y)
             for (int x = 0; x < gx; ++x) {
-                int best = cap + 1;
-                for (int r = 0; r <= cap; ++r) {
-                    const int rx = r, ry = r / wy, rz = r;
-                    const int x0 = (oct & 1) ? x : x - rx, x1 = (oct & 1) ? x + rx : x;
-                    const int y0 = (oct & 2) ? y : y - ry, y1 = (oct & 2) ? y + ry : y;
-                    const int z0 = (oct & 4) ? z : z - rz, z1 = (oct & 4) ? z + rz : z;
-                    if (count(x0, x1, y0, y1, z0, z1) > 0) {
+                int best = vt::kDistCap + 1;
+                for (int r = 0; r <= vt::kDistCap; ++r) {
+                    const int x0 = (oct & 1) ? x : x - r, x1 = (oct & 1) ? x + r : x;
+                    const int y0 = (oct & 2) ? y : y - r, y1 = (oct & 2) ? y + r : y;
+                    const int z0 = (oct & 4) ? z : z - r, z1 = (oct & 4) ? z + r : z;
+                    if (sat.count(x0, x1, y0, y1, z0, z1) > 0) {
                         best = r;
                         break;
                     }
                 }
                 d[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] = (unsigned char)best;
+            }
+    return d;
+}
+
+// Brick distances in voxel layers for octant oct: per brick of the gx*gy*gz
+// brick grid, 0 if the brick holds an occupied voxel, else the smallest E
+// (capped at kVoxCap + 1) for which the brick grown by E voxel layers beyond
+// its far faces across and E / wy layers vertically holds one.  Found by
+// bisection over E with a summed-area table of the voxels: independent of the
+// library's separable passes.
+static std::vector<unsigned char> voxel_cheb(Sat& sat, int gx, int gy, int gz, int wy, int oct) {
+    auto occupied = [&](int bx, int by, int bz, int E) {
+        const int ex = E, ey = E / wy, ez = E;
+        const int x0 = (oct & 1) ? 4 * bx : 4 * bx - ex, x1 = (oct & 1) ? 4 * bx + 3 + ex : 4 * bx + 3;
+        const int y0 = (oct & 2) ? 4 * by : 4 * by - ey, y1 = (oct & 2) ? 4 * by + 3 + ey : 4 * by + 3;
+        const int z0 = (oct & 4) ? 4 * bz : 4 * bz - ez, z1 = (oct & 4) ? 4 * bz + 3 + ez : 4 * bz + 3;
+        return sat.count(x0, x1, y0, y1, z0, z1) > 0;
+    };
+    std::vector<unsigned char> d((size_t)gx * gy * gz);
+    for (int z = 0; z < gz; ++z)
+        for (int y = 0; y < gy; ++y)
+            for (int x = 0; x < gx; ++x) {
+                int v = 0;
+                if (!occupied(x, y, z, 0)) {
+                    int lo = 0, hi = vt::kVoxCap;   // the largest E in [0, kVoxCap] whose box is empty
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) / 2;
+                        if (occupied(x, y, z, mid)) hi = mid - 1;
+                        else lo = mid;
+                    }
+                    v = lo + 1;
+                }
+                d[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] = (unsigned char)v;
             }
     return d;
 }
@@ -81,20 +118,19 @@ static void distances(const int cd[3], const std::vector<unsigned long long>& ma
                       std::vector<unsigned char>& cdist, size_t cstride) {
     const size_t nch = (size_t)cd[0] * cd[1] * cd[2];
     const int gx = cd[0] * 8, gy = cd[1] * 8, gz = cd[2] * 8;
-    std::vector<unsigned char> bocc((size_t)gx * gy * gz), cocc(nch);
-    for (int z = 0; z < gz; ++z)
-        for (int y = 0; y < gy; ++y)
-            for (int x = 0; x < gx; ++x) {
-                size_t ci = (size_t)(x >> 3) + cd[0] * ((size_t)(y >> 3) + (size_t)cd[1] * (z >> 3));
-                unsigned bi = (x & 7) | ((y & 7) << 3) | ((z & 7) << 6);
-                bocc[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] = mask[ci * 512 + bi] != 0;
-                if (mask[ci * 512 + bi]) cocc[ci] = 1;
-            }
+    std::vector<unsigned char> cocc(nch);
+    for (size_t ci = 0; ci < nch; ++ci)
+        for (int bi = 0; bi < 512 && !cocc[ci]; ++bi) cocc[ci] = mask[ci * 512 + bi] != 0;
+    Sat vsat(gx * 4, gy * 4, gz * 4, [&](int x, int y, int z) {
+        const size_t ci = (size_t)(x >> 5) + cd[0] * ((size_t)(y >> 5) + (size_t)cd[1] * (z >> 5));
+        const unsigned bi = ((x >> 2) & 7) | (((y >> 2) & 7) << 3) | (((z >> 2) & 7) << 6);
+        return ((mask[ci * 512 + bi] >> ((x & 3) | ((y & 3) << 2) | ((z & 3) << 4))) & 1ull) != 0;
+    });
     bdist.assign(vt::kOctants * nch * 512, 0);
     cdist.assign(vt::kOctants * cstride, 0);
     for (int o = 0; o < vt::kOctants; ++o) {
-        std::vector<unsigned char> bd = cheb(bocc, gx, gy, gz, vt::flat_y((unsigned)o), o),
-                                   cdd = cheb(cocc, cd[0], cd[1], cd[2], 1, o);
+        std::vector<unsigned char> bd = voxel_cheb(vsat, gx, gy, gz, vt::flat_y((unsigned)o), o),
+                                   cdd = cheb(cocc, cd[0], cd[1], cd[2], o);
         for (int z = 0; z < gz; ++z)
             for (int y = 0; y < gy; ++y)
                 for (int x = 0; x < gx; ++x) {

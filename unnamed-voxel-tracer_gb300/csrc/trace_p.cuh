@@ -311,8 +311,9 @@ __device__ __forceinline__ bool trace_p(const WorldView& w, const Coarse& coarse
 // trace_p (the jump argument holds for any empty axis-aligned box that contains
 // the current cell), with larger jumps and a cheaper unit step:
 //   - an empty chunk is left through the box of chunks ahead within Chebyshev
-//     radius cdist - 1 (all empty), an empty brick through the box of bricks
-//     ahead within radius bdist - 1, both from the ray's octant field (the
+//     radius cdist - 1 (all empty), an empty brick through the box made of
+//     the brick and bdist - 1 voxel layers beyond its far faces (fewer
+//     vertically for rays moving down), both from the ray's octant field (the
 //     ray only moves forwards on every axis, so the exit of a box that extends
 //     forwards from the current unit is the exit of the symmetric box);
 //   - inside an occupied brick only the next-plane index nk and time tm of the
@@ -372,6 +373,18 @@ struct Walker {
         oct = (r.pos[0] ? 1u : 0u) | (r.pos[1] ? 2u : 0u) | (r.pos[2] ? 4u : 0u);
         state = 0;
         return true;
+    }
+
+    // The plane through which the ray leaves, on axis i, the empty box around
+    // cell ci: sh 5, the chunk of ci and the chunks within rad - 1 ahead; sh
+    // 2, the brick of ci and rad - 1 voxel layers beyond its far face
+    // ((rad - 1) / flat_y(oct) vertically; rad >= 1 in an empty brick, so the
+    // quotient is a shift); sh 0, the cell itself (rad 1).
+    __device__ __forceinline__ int exit_plane(int i, int ci, int sh, int rad) const {
+        const int u = ci >> sh;
+        int beyond = (rad - 1) << sh;   // cells beyond the unit's far face
+        if (sh == 2) beyond = i == 1 ? (int)((unsigned)(rad - 1) >> ((oct & 2u) ? 0 : kFlatYShift)) : rad - 1;
+        return r.pos[i] ? ((u + 1) << sh) + beyond : (u << sh) - beyond;
     }
 
     // The brick word wi.  SHARE: the lanes of the warp that look up a word
@@ -477,18 +490,14 @@ struct Walker {
             if (!RUN) return kMore;
           }
         }
-        // leave the empty box reaching rad - 1 units of 2^sh ahead of the unit of c
+        // leave the empty box: the chunk and the chunks within rad - 1 ahead,
+        // or the brick and rad - 1 voxel layers beyond it
         VT_STEP_HOOK(sh == 5 ? 0 : 1);
         int K[3];
         float tK[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            const int u = c[i] >> sh;
-            // a brick distance d promises d-1 bricks ahead across and
-            // (d-1)/flat_y(oct) vertically (the field's weighted Chebyshev
-            // distance; rad >= 1 in an empty unit, so the quotient is a shift)
-            const int ri = (i == 1 && sh == 2) ? (int)((unsigned)(rad - 1) >> ((oct & 2u) ? 0 : kFlatYShift)) + 1 : rad;
-            K[i] = r.pos[i] ? (u + ri) * (1 << sh) : (u - (ri - 1)) * (1 << sh);
+            K[i] = exit_plane(i, c[i], sh, rad);
             tK[i] = ptime(r, i, K[i]);
         }
         const int e = tK[0] < tK[1] ? (tK[0] < tK[2] ? 0 : 2) : (tK[1] < tK[2] ? 1 : 2);
@@ -564,15 +573,13 @@ struct Walker {
 #pragma unroll
             for (int i = 0; i < 3; ++i) c[i] = r.pos[i] ? nk[i] - 1 : nk[i];
         }
-        // leave the box: the voxel (sh 0), or the empty box reaching rad - 1
-        // units of 2^sh ahead of the unit of c
+        // leave the box: the voxel (sh 0, rad 1), or the empty chunk or
+        // brick box as in step()
         int K[3];
         float tK[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            const int u = c[i] >> sh;
-            const int ri = (i == 1 && sh == 2) ? (int)((unsigned)(rad - 1) >> ((oct & 2u) ? 0 : kFlatYShift)) + 1 : rad;
-            K[i] = r.pos[i] ? (u + ri) * (1 << sh) : (u - (ri - 1)) * (1 << sh);
+            K[i] = exit_plane(i, c[i], sh, rad);
             tK[i] = sh == 0 ? tm[i] : ptime(r, i, K[i]);
         }
         const int e = tK[0] < tK[1] ? (tK[0] < tK[2] ? 0 : 2) : (tK[1] < tK[2] ? 1 : 2);

@@ -28,8 +28,9 @@ struct WorldView {
     const unsigned long long* coarse;   // one bit per chunk
     const unsigned* palette;            // 256 RGBA8
     const unsigned char* bdist;         // kOctants fields of nwords bytes (octant-major), per brick:
-                                        // 0 if occupied, else the distance to the nearest occupied
-                                        // brick ahead in that octant (below), capped at kDistCap + 1
+                                        // 0 if occupied, else the distance in voxel layers to the
+                                        // nearest occupied voxel ahead in that octant (below), capped
+                                        // at kVoxCap + 1
     const unsigned char* cdist;         // kOctants fields of cstride bytes, per chunk: same, in chunks
     const float* entities;              // n_entities boxes {lo x, y, z, hi x, y, z}: shadow occluders
     int n_entities;
@@ -41,23 +42,32 @@ struct WorldView {
     unsigned cstride;                   // bytes per chunk-distance field (nchunks rounded up to 16)
 };
 
-// Cap of the empty-space distances: a stored value d >= 1 promises that every
-// brick (chunk) within radius d - 1 ahead is empty.
+// Cap of the chunk distances: a stored value d >= 1 promises that every
+// chunk within radius d - 1 ahead is empty.
 constexpr int kDistCap = 15;
+// Cap of the brick distances, counted in voxel layers: a stored value s >= 1
+// promises that the brick plus s - 1 voxel layers beyond its far faces (fewer
+// vertically, see kFlatY) holds no occupied voxel.  Counting in voxels rather
+// than whole bricks lets a jump out of an empty brick end inside the next
+// occupied brick, at the first layer that can hold a voxel: 32% fewer voxel
+// tests for the primary rays of the 1080p terrain frames.
+constexpr int kVoxCap = 63;
 // Distances are kept per direction octant.  Field o (bit i set: the ray moves
-// towards +i) of a brick b holds min over occupied bricks b' with
-// sign(b'_i - b_i) in {0, that direction} of the weighted distance below: it
-// looks only where a ray of that octant can go.  A ray leaving b moves away
-// from b on every axis, so the empty box it may jump through only has to
-// extend forwards; rays that leave the terrain (shadow rays toward the sun,
+// towards +i) of a chunk c holds min over occupied chunks c' with
+// sign(c'_i - c_i) in {0, that direction} of max(|dx|, |dy|, |dz|); field o of
+// a brick holds the same over occupied voxels, in voxel layers beyond the
+// brick's far faces, with the vertical weight below: it looks only where a
+// ray of that octant can go.  A ray leaving a cell moves away from it on
+// every axis, so the empty box it may jump through only has to extend
+// forwards; rays that leave the terrain (shadow rays toward the sun,
 // primary rays above the ground) see the open space in front of them instead
 // of the terrain they came from.
 constexpr int kOctants = 8;
 __host__ __device__ inline unsigned cdist_stride(unsigned nchunks) { return (nchunks + 15u) / 16u * 16u; }
 // The brick distance of the octants whose rays move down (-y) weighs vertical
-// offsets by kFlatY: d = min over occupied bricks of max(|dx|, kFlatY*|dy|,
-// |dz|).  Its empty box is flat and wide (radius d-1 across, (d-1)/kFlatY up
-// and down), which suits rays that descend towards terrain.  The octants of
+// offsets by kFlatY: s = min over occupied voxels of max(dx, kFlatY*dy, dz).
+// Its empty box is flat and wide (s-1 layers across, (s-1)/kFlatY up and
+// down), which suits rays that descend towards terrain.  The octants of
 // rays that move up (away from the ground: shadow rays towards a sun above
 // the horizon) use plain Chebyshev (25% fewer brick jumps for the shadow rays
 // of the 1080p terrain frames), as does the chunk distance.
@@ -146,7 +156,7 @@ struct vt_world {
     unsigned* d_palette = nullptr;
     unsigned char* d_bdist = nullptr;
     unsigned char* d_cdist = nullptr;
-    unsigned char* d_dtmp = nullptr;   // x (2 fields) and y (4 fields) pass results of the brick distances (kept)
+    unsigned char* d_dtmp = nullptr;   // x (2 fields, 16 B/brick) and y (4 fields, 4 B/brick) pass results of the brick distances (kept)
     unsigned char* d_ctmp = nullptr;   // the same 6 fields for the chunk distances
     int* d_edit = nullptr;             // {x, y, z, valid} of the last device-side edit
     float* d_entities = nullptr;       // kMaxEntities boxes of 6 floats

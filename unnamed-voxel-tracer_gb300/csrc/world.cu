@@ -86,73 +86,169 @@ __global__ void __launch_bounds__(512) k_set_voxel(WorldView w, unsigned long lo
 }
 
 // Empty-space distances, per direction octant.  For the octant with signs s,
-// the weighted Chebyshev distance from a brick (chunk) to the nearest
-// occupied one ahead is separable:
-//     min over b' ahead of max(|dx|, w|dy|, |dz|)
-//   = min_{dz ahead} max(|dz|, min_{dy ahead} max(w|dy|, min_{dx ahead} max(|dx|, occ(b')))),
-// "ahead" meaning 0 <= s_i * d_i <= kDistCap.  Each pass is one of those
-// one-sided 1-D min-max filters; values are capped at kDistCap + 1 ("nothing
-// occupied within kDistCap").  The x pass depends on s_x only (2 fields), the
-// y pass on s_x, s_y (4 fields), the z pass on all three (8 fields).  Cells
-// outside the grid count as empty.
-__device__ __forceinline__ unsigned brick_index(int bx, int by, int bz, int CX, int CY) {
-    const unsigned ci = (unsigned)(bx >> 3) + (unsigned)CX * ((unsigned)(by >> 3) + (unsigned)CY * (unsigned)(bz >> 3));
-    return ci * 512u + (unsigned)((bx & 7) | ((by & 7) << 3) | ((bz & 7) << 6));
-}
-
-// level 0: bricks (grid = 8 * chunk counts), level 1: chunks.  blockIdx.y is
-// the output field v: bit i of v gives the direction of axis i (1: +) for
-// axes 0..axis; the pass reads input field v & ((1 << axis) - 1) (pass 0
-// reads the mask words / coarse bits instead).  Fields are `stride` bytes
-// apart.  The pass covers the box [lo, lo + ext) of the grid (clipped to it);
-// when `d_cell` is given, {x, y, z, valid} of an edited voxel in device
-// memory, the box is taken relative to that voxel's brick and skipped when
-// !valid.
-__global__ void k_dist_pass(const unsigned long long* __restrict__ mask, const unsigned long long* __restrict__ coarse,
-                            const unsigned char* __restrict__ in, unsigned char* __restrict__ out, int level, int axis,
-                            int CX, int CY, int CZ, int3 lo, int3 ext, const int* __restrict__ d_cell, size_t stride) {
-    const int gx = level == 0 ? CX * 8 : CX, gy = level == 0 ? CY * 8 : CY, gz = level == 0 ? CZ * 8 : CZ;
-    if (d_cell) {
-        if (!d_cell[3]) return;
-        lo.x += d_cell[0] >> 2;
-        lo.y += d_cell[1] >> 2;
-        lo.z += d_cell[2] >> 2;
-    }
+// a weighted Chebyshev distance to the nearest occupied cell ahead is
+// separable:
+//     min over c' ahead of max(|dx|, w|dy|, |dz|)
+//   = min_{dz ahead} max(|dz|, min_{dy ahead} max(w|dy|, min_{dx ahead} max(|dx|, occ(c')))),
+// so each field is three one-sided 1-D min-max passes, x, then y, then z.
+// The x pass depends on s_x only (2 fields), the y pass on s_x, s_y (4 fields),
+// the z pass on all three (8 fields).  Cells outside the grid count as empty.
+//
+// Chunk level: chunks to chunks, "ahead" meaning 0 <= s_i * d_i <= kDistCap,
+// capped at kDistCap + 1.  blockIdx.y is the output field v: bit i of v gives
+// the direction of axis i (1: +) for axes 0..axis; the pass reads input field
+// v & ((1 << axis) - 1) (pass 0 reads the coarse bits instead).  Fields are
+// `stride` bytes apart.  The pass covers the whole chunk grid.
+__global__ void k_dist_pass(const unsigned long long* __restrict__ coarse, const unsigned char* __restrict__ in,
+                            unsigned char* __restrict__ out, int axis, int CX, int CY, int CZ, size_t stride) {
     const unsigned v = blockIdx.y;
     const bool fwd = ((v >> axis) & 1u) != 0u;
     if (axis > 0) in += (size_t)(v & ((1u << axis) - 1u)) * stride;
     out += (size_t)v * stride;
     const int dlo = fwd ? 0 : -kDistCap, dhi = fwd ? kDistCap : 0;
-    const int wgt = level == 0 && axis == 1 ? flat_y(v) : 1;  // v's bit 1 is the y direction
-    const size_t total = (size_t)ext.x * ext.y * ext.z;
+    const int g[3] = {CX, CY, CZ};
+    const size_t total = (size_t)CX * CY * CZ;
     for (size_t lin = blockIdx.x * (size_t)blockDim.x + threadIdx.x; lin < total; lin += (size_t)gridDim.x * blockDim.x) {
-        const int x = lo.x + (int)(lin % ext.x), y = lo.y + (int)((lin / ext.x) % ext.y),
-                  z = lo.z + (int)(lin / ((size_t)ext.x * ext.y));
-        if (x < 0 || y < 0 || z < 0 || x >= gx || y >= gy || z >= gz) continue;
-        const int g[3] = {gx, gy, gz};
-        int p[3] = {x, y, z};
+        int p[3] = {(int)(lin % CX), (int)((lin / CX) % CY), (int)(lin / ((size_t)CX * CY))};
         const int u = p[axis];
         int best = kDistCap + 1;
         for (int dd = dlo; dd <= dhi; ++dd) {
             const int q = u + dd;
             if (q < 0 || q >= g[axis]) continue;
             p[axis] = q;
-            unsigned idx;
-            if (level == 0) idx = brick_index(p[0], p[1], p[2], CX, CY);
-            else idx = (unsigned)p[0] + (unsigned)CX * ((unsigned)p[1] + (unsigned)CY * (unsigned)p[2]);
-            int val;
-            if (axis == 0) {
-                const bool occ = level == 0 ? mask[idx] != 0ull : ((coarse[idx >> 6] >> (idx & 63u)) & 1ull) != 0ull;
-                val = occ ? 0 : kDistCap + 1;
-            } else {
-                val = in[idx];
-            }
-            best = min(best, max(wgt * abs(dd), val));
+            const unsigned idx = (unsigned)p[0] + (unsigned)CX * ((unsigned)p[1] + (unsigned)CY * (unsigned)p[2]);
+            const int val = axis == 0 ? (((coarse[idx >> 6] >> (idx & 63u)) & 1ull) ? 0 : kDistCap + 1) : (int)in[idx];
+            best = min(best, max(abs(dd), val));
         }
-        p[axis] = u;
-        const unsigned oidx = level == 0 ? brick_index(x, y, z, CX, CY)
-                                         : (unsigned)x + (unsigned)CX * ((unsigned)y + (unsigned)CY * (unsigned)z);
-        out[oidx] = (unsigned char)best;
+        out[lin] = (unsigned char)best;
+    }
+}
+
+// Brick level, in voxels.  Field o of brick b holds
+//     min(kVoxCap + 1, min over occupied voxels q ahead of b of max(dx, wy*dy, dz)),
+// wy = flat_y(o), where d_i is the number of voxel layers between b's far
+// face on axis i and q (0 when q lies within b's extent on that axis) and
+// "ahead" means q is not behind b's near face on any axis.  0 marks an
+// occupied brick; a value s >= 1 promises that b plus s - 1 layers beyond its
+// far faces across and (s - 1) / wy layers vertically holds no occupied
+// voxel.  Each pass coarsens one axis from voxels to bricks:
+//   x: X(bx, qy, qz), 2 fields: layers from brick bx's far x face to the first
+//      occupied voxel of row (qy, qz) (read from the mask words);
+//   y: Y(bx, by, qz), 4 fields: min over qy of max(wy*dy, X(bx, qy, qz));
+//   z: the brick field, 8 fields: min over qz of max(dz, Y(bx, by, qz)).
+// The intermediates are x-fastest arrays: X over (GX bricks, GY*4, GZ*4
+// voxels), Y over (GX, GY bricks, GZ*4 voxels).  Each pass covers a box of
+// its own output grid, [lo, lo + ext) clipped to the grid; with `d_cell`
+// ({x, y, z, valid} of an edited voxel in device memory) the box is taken
+// relative to that voxel's brick (brick axes) or the brick's first voxel
+// (voxel axes), and skipped when !valid.
+__device__ __forceinline__ unsigned brick_index(int bx, int by, int bz, int CX, int CY) {
+    const unsigned ci = (unsigned)(bx >> 3) + (unsigned)CX * ((unsigned)(by >> 3) + (unsigned)CY * (unsigned)(bz >> 3));
+    return ci * 512u + (unsigned)((bx & 7) | ((by & 7) << 3) | ((bz & 7) << 6));
+}
+
+struct BrickGrid {
+    int CX, CY, CZ;   // chunks
+    int GX, GY, GZ;   // bricks
+};
+
+__device__ __forceinline__ bool box_cell(size_t lin, int3 lo, int3 ext, int3 g, int& x, int& y, int& z) {
+    x = lo.x + (int)(lin % ext.x);
+    y = lo.y + (int)((lin / ext.x) % ext.y);
+    z = lo.z + (int)(lin / ((size_t)ext.x * ext.y));
+    return x >= 0 && y >= 0 && z >= 0 && x < g.x && y < g.y && z < g.z;
+}
+
+__device__ __forceinline__ int3 edit_origin(int3 lo, const int* d_cell, bool vx, bool vy, bool vz) {
+    const int bx = d_cell[0] >> 2, by = d_cell[1] >> 2, bz = d_cell[2] >> 2;
+    lo.x += vx ? 4 * bx : bx;
+    lo.y += vy ? 4 * by : by;
+    lo.z += vz ? 4 * bz : bz;
+    return lo;
+}
+
+__global__ void k_bdist_x(const unsigned long long* __restrict__ mask, unsigned char* __restrict__ xf, BrickGrid b,
+                          int3 lo, int3 ext, const int* __restrict__ d_cell) {
+    if (d_cell) {
+        if (!d_cell[3]) return;
+        lo = edit_origin(lo, d_cell, false, true, true);
+    }
+    const bool fwd = blockIdx.y != 0;
+    const int3 g = make_int3(b.GX, b.GY * 4, b.GZ * 4);
+    const size_t fsize = (size_t)g.x * g.y * g.z;
+    xf += blockIdx.y * fsize;
+    const size_t total = (size_t)ext.x * ext.y * ext.z;
+    for (size_t lin = blockIdx.x * (size_t)blockDim.x + threadIdx.x; lin < total; lin += (size_t)gridDim.x * blockDim.x) {
+        int bx, qy, qz;
+        if (!box_cell(lin, lo, ext, g, bx, qy, qz)) continue;
+        const unsigned row = 4u * (unsigned)(qy & 3) + 16u * (unsigned)(qz & 3);
+        int best = kVoxCap + 1;
+        for (int j = 0;; ++j) {
+            const int nb = fwd ? bx + j : bx - j;
+            // a voxel of brick nb lies at least 4j - 3 layers beyond bx's far face
+            if (max(0, 4 * j - 3) >= best || nb < 0 || nb >= g.x) break;
+            const unsigned bits = (unsigned)(mask[brick_index(nb, qy >> 2, qz >> 2, b.CX, b.CY)] >> row) & 15u;
+            if (bits) {
+                best = fwd ? max(0, 4 * j + (__ffs(bits) - 1) - 3) : max(0, 4 * j - (31 - __clz(bits)));
+                break;
+            }
+        }
+        xf[(size_t)bx + (size_t)g.x * ((size_t)qy + (size_t)g.y * qz)] = (unsigned char)min(best, kVoxCap + 1);
+    }
+}
+
+__global__ void k_bdist_y(const unsigned char* __restrict__ xf, unsigned char* __restrict__ yf, BrickGrid b, int3 lo,
+                          int3 ext, const int* __restrict__ d_cell) {
+    if (d_cell) {
+        if (!d_cell[3]) return;
+        lo = edit_origin(lo, d_cell, false, false, true);
+    }
+    const unsigned v = blockIdx.y;   // bit 0: x direction, bit 1: y direction
+    const bool fwd = (v & 2u) != 0u;
+    const int wy = flat_y(v);
+    const int Y = b.GY * 4;
+    const int3 g = make_int3(b.GX, b.GY, b.GZ * 4);
+    xf += (size_t)(v & 1u) * ((size_t)b.GX * Y * g.z);
+    yf += (size_t)v * ((size_t)g.x * g.y * g.z);
+    const size_t total = (size_t)ext.x * ext.y * ext.z;
+    for (size_t lin = blockIdx.x * (size_t)blockDim.x + threadIdx.x; lin < total; lin += (size_t)gridDim.x * blockDim.x) {
+        int bx, by, qz;
+        if (!box_cell(lin, lo, ext, g, bx, by, qz)) continue;
+        int best = kVoxCap + 1;
+        for (int t = 0;; ++t) {
+            const int dy = max(0, t - 3);
+            const int qy = fwd ? 4 * by + t : 4 * by + 3 - t;
+            if (wy * dy >= best || qy < 0 || qy >= Y) break;
+            best = min(best, max(wy * dy, (int)xf[(size_t)bx + (size_t)g.x * ((size_t)qy + (size_t)Y * qz)]));
+        }
+        yf[(size_t)bx + (size_t)g.x * ((size_t)by + (size_t)g.y * qz)] = (unsigned char)best;
+    }
+}
+
+__global__ void k_bdist_z(const unsigned char* __restrict__ yf, unsigned char* __restrict__ out, BrickGrid b, int3 lo,
+                          int3 ext, const int* __restrict__ d_cell, size_t stride) {
+    if (d_cell) {
+        if (!d_cell[3]) return;
+        lo = edit_origin(lo, d_cell, false, false, false);
+    }
+    const unsigned v = blockIdx.y;   // the octant
+    const bool fwd = (v & 4u) != 0u;
+    const int Z = b.GZ * 4;
+    const int3 g = make_int3(b.GX, b.GY, b.GZ);
+    yf += (size_t)(v & 3u) * ((size_t)b.GX * b.GY * Z);
+    out += (size_t)v * stride;
+    const size_t total = (size_t)ext.x * ext.y * ext.z;
+    for (size_t lin = blockIdx.x * (size_t)blockDim.x + threadIdx.x; lin < total; lin += (size_t)gridDim.x * blockDim.x) {
+        int bx, by, bz;
+        if (!box_cell(lin, lo, ext, g, bx, by, bz)) continue;
+        int best = kVoxCap + 1;
+        for (int t = 0;; ++t) {
+            const int dz = max(0, t - 3);
+            const int qz = fwd ? 4 * bz + t : 4 * bz + 3 - t;
+            if (dz >= best || qz < 0 || qz >= Z) break;
+            best = min(best, max(dz, (int)yf[(size_t)bx + (size_t)g.x * ((size_t)by + (size_t)g.y * qz)]));
+        }
+        out[brick_index(bx, by, bz, b.CX, b.CY)] = (unsigned char)best;
     }
 }
 
@@ -164,62 +260,64 @@ unsigned dist_blocks(size_t n) {
     return (unsigned)std::min<size_t>((n + kDistThreads - 1) / kDistThreads, 65535u * 4u);
 }
 
-// The three passes of one level over a box each: x into 2 fields of tmp, y
-// into the 4 fields after them, z into the 8 output fields.
-void level_passes(vt_world* w, cudaStream_t st, int level, unsigned char* tmp, unsigned char* out, size_t stride,
-                  const int3 lo[3], const int3 ext[3], const int* d_cell) {
-    const int CX = w->cdim[0], CY = w->cdim[1], CZ = w->cdim[2];
-    unsigned char* fx = tmp;
-    unsigned char* fy = tmp + 2 * stride;
-    auto grid = [&](int3 e, int fields) {
-        return dim3(dist_blocks((size_t)e.x * e.y * e.z), (unsigned)fields);
-    };
-    k_dist_pass<<<grid(ext[0], 2), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, nullptr, fx, level, 0, CX, CY, CZ,
-                                                         lo[0], ext[0], d_cell, stride);
-    k_dist_pass<<<grid(ext[1], 4), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, fx, fy, level, 1, CX, CY, CZ,
-                                                         lo[1], ext[1], d_cell, stride);
-    k_dist_pass<<<grid(ext[2], 8), kDistThreads, 0, st>>>(w->d_mask, w->d_coarse, fy, out, level, 2, CX, CY, CZ,
-                                                         lo[2], ext[2], d_cell, stride);
-}
-
-// The chunk level over the whole chunk grid (at most a few tens of thousands
-// of cells: cheap enough to redo after any edit).
-void chunk_passes(vt_world* w, cudaStream_t st) {
-    const int3 o = make_int3(0, 0, 0), g = make_int3(w->cdim[0], w->cdim[1], w->cdim[2]);
-    const int3 lo[3] = {o, o, o}, ext[3] = {g, g, g};
-    level_passes(w, st, 1, w->d_ctmp, w->d_cdist, cdist_stride((unsigned)w->nchunks), lo, ext, nullptr);
-}
-
 size_t volume(int3 e) { return (size_t)e.x * e.y * e.z; }
 
-// The brick level, each pass over its own box.  The intermediates stay valid
+// The chunk level over the whole chunk grid (at most a few tens of thousands
+// of cells: cheap enough to redo after any edit): x into 2 fields of tmp, y
+// into the 4 fields after them, z into the 8 output fields.
+void chunk_passes(vt_world* w, cudaStream_t st) {
+    const int CX = w->cdim[0], CY = w->cdim[1], CZ = w->cdim[2];
+    const size_t stride = cdist_stride((unsigned)w->nchunks);
+    unsigned char* fx = w->d_ctmp;
+    unsigned char* fy = w->d_ctmp + 2 * stride;
+    const unsigned nb = dist_blocks(w->nchunks);
+    k_dist_pass<<<dim3(nb, 2), kDistThreads, 0, st>>>(w->d_coarse, nullptr, fx, 0, CX, CY, CZ, stride);
+    k_dist_pass<<<dim3(nb, 4), kDistThreads, 0, st>>>(w->d_coarse, fx, fy, 1, CX, CY, CZ, stride);
+    k_dist_pass<<<dim3(nb, 8), kDistThreads, 0, st>>>(w->d_coarse, fy, w->d_cdist, 2, CX, CY, CZ, stride);
+}
+
+// The brick level, each pass over its own box (x: bricks x voxels x voxels,
+// y: bricks x bricks x voxels, z: bricks).  The intermediates stay valid
 // between calls, which is what lets an edit recompute only the boxes it can
 // change.
 void brick_passes(vt_world* w, cudaStream_t st, const int3 lo[3], const int3 ext[3], const int* d_cell) {
-    level_passes(w, st, 0, w->d_dtmp, w->d_bdist, w->nchunks * kBricksPerChunk, lo, ext, d_cell);
+    const BrickGrid b = {w->cdim[0], w->cdim[1], w->cdim[2], w->cdim[0] * 8, w->cdim[1] * 8, w->cdim[2] * 8};
+    const size_t nb = w->nchunks * kBricksPerChunk;
+    unsigned char* xf = w->d_dtmp;             // 2 fields of 16 bytes per brick
+    unsigned char* yf = w->d_dtmp + 32 * nb;   // 4 fields of 4 bytes per brick
+    if (volume(ext[0]))
+        k_bdist_x<<<dim3(dist_blocks(volume(ext[0])), 2), kDistThreads, 0, st>>>(w->d_mask, xf, b, lo[0], ext[0], d_cell);
+    if (volume(ext[1]))
+        k_bdist_y<<<dim3(dist_blocks(volume(ext[1])), 4), kDistThreads, 0, st>>>(xf, yf, b, lo[1], ext[1], d_cell);
+    if (volume(ext[2]))
+        k_bdist_z<<<dim3(dist_blocks(volume(ext[2])), 8), kDistThreads, 0, st>>>(yf, w->d_bdist, b, lo[2], ext[2],
+                                                                                 d_cell, nb);
 }
 
 // After the bricks of box [blo, blo + bext) changed occupancy only these
-// cells can change: the x pass in the box +- (R, 0, 0), the y pass in the box
-// +- (R, RY, 0), the z pass in the box +- (R, RY, R), with R = RY = kDistCap
-// (the upward octants' fields weigh y offsets by 1, so their y pass reaches
-// as far as the others).  Recomputing exactly those boxes, in pass order, from
-// the current masks leaves every buffer equal to a full rebuild.
+// cells can change (R bricks: the farthest any pass looks, kVoxCap + 3 voxel
+// layers, rounded up, plus one): the x pass in the box +- R bricks in x over
+// the edited bricks' voxel rows, the y pass +- R bricks in x and y over their
+// voxel layers in z, the z pass +- R bricks on every axis.  Recomputing those
+// boxes, in pass order, from the current masks leaves every buffer equal to
+// a full rebuild.
 void edit_boxes(int3 blo, int3 bext, int3 lo[3], int3 ext[3]) {
-    const int R = kDistCap, RY = kDistCap / flat_y(2u);
-    lo[0] = make_int3(blo.x - R, blo.y, blo.z);
-    ext[0] = make_int3(bext.x + 2 * R, bext.y, bext.z);
-    lo[1] = make_int3(blo.x - R, blo.y - RY, blo.z);
-    ext[1] = make_int3(bext.x + 2 * R, bext.y + 2 * RY, bext.z);
-    lo[2] = make_int3(blo.x - R, blo.y - RY, blo.z - R);
-    ext[2] = make_int3(bext.x + 2 * R, bext.y + 2 * RY, bext.z + 2 * R);
+    const int R = (kVoxCap + 3) / 4 + 1;
+    lo[0] = make_int3(blo.x - R, 4 * blo.y, 4 * blo.z);
+    ext[0] = make_int3(bext.x + 2 * R, 4 * bext.y, 4 * bext.z);
+    lo[1] = make_int3(blo.x - R, blo.y - R, 4 * blo.z);
+    ext[1] = make_int3(bext.x + 2 * R, bext.y + 2 * R, 4 * bext.z);
+    lo[2] = make_int3(blo.x - R, blo.y - R, blo.z - R);
+    ext[2] = make_int3(bext.x + 2 * R, bext.y + 2 * R, bext.z + 2 * R);
 }
 
 }  // namespace
 
 vt_status rebuild_distances(vt_world* w, cudaStream_t st) {
-    const int3 o = make_int3(0, 0, 0), g = make_int3(w->cdim[0] * 8, w->cdim[1] * 8, w->cdim[2] * 8);
-    const int3 lo[3] = {o, o, o}, ext[3] = {g, g, g};
+    const int GX = w->cdim[0] * 8, GY = w->cdim[1] * 8, GZ = w->cdim[2] * 8;
+    const int3 o = make_int3(0, 0, 0);
+    const int3 lo[3] = {o, o, o};
+    const int3 ext[3] = {make_int3(GX, 4 * GY, 4 * GZ), make_int3(GX, GY, 4 * GZ), make_int3(GX, GY, GZ)};
     brick_passes(w, st, lo, ext, nullptr);
     chunk_passes(w, st);
     VT_CUDA(w->ctx, cudaGetLastError());
@@ -331,7 +429,7 @@ vt_status vt_world_create(vt_ctx* ctx, const vt_world_desc* desc, vt_world** out
         (e = vt::dev_alloc(&w->d_palette, 256 * sizeof(unsigned))) != cudaSuccess ||
         (e = vt::dev_alloc(&w->d_bdist, kOctants * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
         (e = vt::dev_alloc(&w->d_cdist, kOctants * (size_t)cdist_stride((unsigned)w->nchunks))) != cudaSuccess ||
-        (e = vt::dev_alloc(&w->d_dtmp, 6 * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_dtmp, 48 * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
         (e = vt::dev_alloc(&w->d_ctmp, 6 * (size_t)cdist_stride((unsigned)w->nchunks))) != cudaSuccess ||
         (e = vt::dev_alloc(&w->d_edit, 4 * sizeof(int))) != cudaSuccess ||
         (e = vt::dev_alloc(&w->d_entities, kMaxEntities * 6 * sizeof(float))) != cudaSuccess ||
