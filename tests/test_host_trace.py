@@ -119,6 +119,30 @@ def test_far_origins_and_unnormalised_directions(ht, oracle, vtlib):
     assert (got["face"] != 0xFF).sum() > 1500
 
 
+def test_inside_origins_extreme_directions(ht, oracle, vtlib):
+    """Origins inside the grid, on and near the one-cell margin of the walk's
+    inside-start shortcut, with direction components from 1e-38 to 1e38
+    (their reciprocals overflow, underflow or stay ordinary) and zero."""
+    dims = (64, 48, 72)
+    d = vtlib.gen_desc(dims, scale=0.5, seed=11, trees=8, caves=True)
+    mats = vtlib.gen_world(d)
+    rng = np.random.default_rng(11)
+    n = 8000
+    o = rng.uniform([0.0, 0.0, 0.0], dims, (n, 3))
+    k = rng.random((n, 3))
+    edge = np.array(dims, np.float64)
+    o = np.where(k < 0.15, rng.choice([0.0, 0.5, 1.0, 1.0001, 0.9999], (n, 3)), o)
+    o = np.where(k > 0.85, edge - rng.choice([0.0, 0.5, 1.0, 1.0001, 0.9999], (n, 3)), o)
+    mags = np.array([0.0, 1e-38, 1e-30, 1e-8, 1.0, 1e8, 1e30, 1e38])
+    dirs = rng.normal(size=(n, 3))
+    pick = rng.random((n, 3)) < 0.3
+    dirs = np.where(pick, np.sign(dirs) * rng.choice(mags, (n, 3)), dirs)
+    o, dirs = np.ascontiguousarray(o, np.float32), np.ascontiguousarray(dirs, np.float32)
+    check(ht, oracle, mats, o, dirs, 5000)
+    got, _ = run_host(ht, mats, o, dirs, 5000, 1)
+    assert (got["face"] != 0xFF).sum() > 1000
+
+
 def test_counters_match_oracle(ht, oracle, vtlib):
     d = vtlib.gen_desc((128, 64, 96), scale=0.5, seed=4, trees=5)
     mats = vtlib.gen_world(d)

@@ -122,6 +122,25 @@ __device__ __forceinline__ int advance_axis(const PRay& r, int i, int lo, int K,
 
 // Start cell of a ray against the grid box [0, D).  Returns false on a miss.
 __device__ __forceinline__ bool pray_start(const PRay& r, const int D[3], int c[3], float& t0, int& axis0) {
+    // An origin at least one cell inside the grid on every axis (secondary
+    // rays, cameras inside the world) starts in its own cell at t = 0 when
+    // every reciprocal lies in [2^-100, 2^100] in magnitude: then o * inv
+    // neither overflows nor underflows, its rounding error (below 2^-11 |inv|
+    // for o < 2^13) is smaller than the one-cell margin times |inv|, so the
+    // entry planes are crossed at negative times and the exit planes at
+    // positive ones, and the box test below would take its else branch with
+    // the same result.  Anything else (NaN or infinite reciprocals included)
+    // takes the box test.
+    if (r.o[0] >= 1.0f && r.o[1] >= 1.0f && r.o[2] >= 1.0f && r.o[0] <= (float)(D[0] - 1) &&
+        r.o[1] <= (float)(D[1] - 1) && r.o[2] <= (float)(D[2] - 1) && fabsf(r.inv[0]) <= 0x1p100f &&
+        fabsf(r.inv[1]) <= 0x1p100f && fabsf(r.inv[2]) <= 0x1p100f && fabsf(r.inv[0]) >= 0x1p-100f &&
+        fabsf(r.inv[1]) >= 0x1p-100f && fabsf(r.inv[2]) >= 0x1p-100f) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) c[i] = __float2int_rd(r.o[i]);
+        t0 = 0.0f;
+        axis0 = 0;
+        return true;
+    }
     float tin[3], tout[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
