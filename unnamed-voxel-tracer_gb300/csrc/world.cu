@@ -295,14 +295,15 @@ void brick_passes(vt_world* w, cudaStream_t st, const int3 lo[3], const int3 ext
 }
 
 // After the bricks of box [blo, blo + bext) changed occupancy only these
-// cells can change (R bricks: the farthest any pass looks, kVoxCap + 3 voxel
-// layers, rounded up, plus one): the x pass in the box +- R bricks in x over
-// the edited bricks' voxel rows, the y pass +- R bricks in x and y over their
-// voxel layers in z, the z pass +- R bricks on every axis.  Recomputing those
-// boxes, in pass order, from the current masks leaves every buffer equal to
-// a full rebuild.
+// cells can change (R bricks: a pass stops before a layer kVoxCap + 1 beyond
+// the far face, so it reads at most kVoxCap + 3 layers past the near face,
+// which reaches R = (kVoxCap + 3) / 4 bricks away): the x pass in the box
+// +- R bricks in x over the edited bricks' voxel rows, the y pass +- R bricks
+// in x and y over their voxel layers in z, the z pass +- R bricks on every
+// axis.  Recomputing those boxes, in pass order, from the current masks
+// leaves every buffer equal to a full rebuild.
 void edit_boxes(int3 blo, int3 bext, int3 lo[3], int3 ext[3]) {
-    const int R = (kVoxCap + 3) / 4 + 1;
+    const int R = (kVoxCap + 3) / 4;
     lo[0] = make_int3(blo.x - R, 4 * blo.y, 4 * blo.z);
     ext[0] = make_int3(bext.x + 2 * R, 4 * bext.y, 4 * bext.z);
     lo[1] = make_int3(blo.x - R, blo.y - R, 4 * blo.z);
