@@ -503,11 +503,13 @@ vt_status vt_edit(vt_ctx* ctx, vt_world* world, const vt_camera* cam, int32_t ma
  * h_brick gets 8 fields of nchunks*512 bytes (chunk-major, brick bx + 8*(by
  * + 8*bz)), h_chunk 8 fields of nchunks bytes.  Entry of octant o: 0 if
  * occupied; for a chunk, min over occupied chunks ahead in that octant of
- * max(|dx|, |dy|, |dz|), capped at 16; for a brick, min over occupied voxels
- * ahead of max(dx, w*dy, dz), d_i counting the voxel layers between the
- * brick's far face and the voxel (0 within the brick's extent), w = 4 for the
- * octants moving -y and 1 for those moving +y, capped at 64.  For tests and
- * tools. */
+ * max(|dx|, |dy|, |dz|), capped at 16; for a brick, s | shape << 6 where s is
+ * the min over occupied voxels ahead of max(dx, w*dy, dz), d_i counting the
+ * voxel layers between the brick's far face and the voxel (0 within the
+ * brick's extent), w = 2^shape, capped at 63: shape 0 for the octants moving
+ * +y, and for those moving -y the shape 0..3 whose box (4 + s - 1 voxels
+ * across, 4 + ((s - 1) >> shape) vertically) has the largest volume, the
+ * smallest shape on a tie.  For tests and tools. */
 vt_status vt_world_download_distances(vt_world* world, uint8_t* h_brick, size_t brick_bytes, uint8_t* h_chunk,
                                       size_t chunk_bytes);
 

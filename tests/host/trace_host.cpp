@@ -80,14 +80,17 @@ static std::vector<unsigned char> cheb(const std::vector<unsigned char>& occ, in
 }
 
 // Brick distances in voxel layers for octant oct: per brick of the gx*gy*gz
-// brick grid, 0 if the brick holds an occupied voxel, else the smallest E
-// (capped at kVoxCap + 1) for which the brick grown by E voxel layers beyond
-// its far faces across and E / wy layers vertically holds one.  Found by
-// bisection over E with a summed-area table of the voxels: independent of the
-// library's separable passes.
-static std::vector<unsigned char> voxel_cheb(Sat& sat, int gx, int gy, int gz, int wy, int oct) {
+// brick grid, 0 if the brick holds an occupied voxel, else s | shape << 6
+// where s is the smallest E (capped at kVoxCap + 1) for which the brick grown
+// by E voxel layers beyond its far faces across and E >> shape layers
+// vertically holds one: shape 0 for the octants moving +y, else the shape
+// 0..3 whose empty box is largest (box_score; the first on a tie).  Found by
+// bisection over E with a summed-area table of the voxels: independent of
+// the library's separable passes.
+static std::vector<unsigned char> voxel_cheb(Sat& sat, int gx, int gy, int gz, int oct) {
+    int shape = 0;
     auto occupied = [&](int bx, int by, int bz, int E) {
-        const int ex = E, ey = E / wy, ez = E;
+        const int ex = E, ey = E >> shape, ez = E;
         const int x0 = (oct & 1) ? 4 * bx : 4 * bx - ex, x1 = (oct & 1) ? 4 * bx + 3 + ex : 4 * bx + 3;
         const int y0 = (oct & 2) ? 4 * by : 4 * by - ey, y1 = (oct & 2) ? 4 * by + 3 + ey : 4 * by + 3;
         const int z0 = (oct & 4) ? 4 * bz : 4 * bz - ez, z1 = (oct & 4) ? 4 * bz + 3 + ez : 4 * bz + 3;
@@ -97,15 +100,18 @@ static std::vector<unsigned char> voxel_cheb(Sat& sat, int gx, int gy, int gz, i
     for (int z = 0; z < gz; ++z)
         for (int y = 0; y < gy; ++y)
             for (int x = 0; x < gx; ++x) {
-                int v = 0;
-                if (!occupied(x, y, z, 0)) {
+                int v = 0, best_score = -1;
+                for (shape = 0; shape < ((oct & 2) ? 1 : vt::kBoxShapes) && !occupied(x, y, z, 0); ++shape) {
                     int lo = 0, hi = vt::kVoxCap;   // the largest E in [0, kVoxCap] whose box is empty
                     while (lo < hi) {
                         const int mid = (lo + hi + 1) / 2;
                         if (occupied(x, y, z, mid)) hi = mid - 1;
                         else lo = mid;
                     }
-                    v = lo + 1;
+                    if (vt::box_score(lo + 1, shape) > best_score) {
+                        best_score = vt::box_score(lo + 1, shape);
+                        v = (lo + 1) | (shape << 6);
+                    }
                 }
                 d[(size_t)x + (size_t)gx * ((size_t)y + (size_t)gy * z)] = (unsigned char)v;
             }
@@ -129,7 +135,7 @@ static void distances(const int cd[3], const std::vector<unsigned long long>& ma
     bdist.assign(vt::kOctants * nch * 512, 0);
     cdist.assign(vt::kOctants * cstride, 0);
     for (int o = 0; o < vt::kOctants; ++o) {
-        std::vector<unsigned char> bd = voxel_cheb(vsat, gx, gy, gz, vt::flat_y((unsigned)o), o),
+        std::vector<unsigned char> bd = voxel_cheb(vsat, gx, gy, gz, o),
                                    cdd = cheb(cocc, cd[0], cd[1], cd[2], o);
         for (int z = 0; z < gz; ++z)
             for (int y = 0; y < gy; ++y)

@@ -396,13 +396,16 @@ struct Walker {
 
     // The plane through which the ray leaves, on axis i, the empty box around
     // cell ci: sh 5, the chunk of ci and the chunks within rad - 1 ahead; sh
-    // 2, the brick of ci and rad - 1 voxel layers beyond its far face
-    // ((rad - 1) / flat_y(oct) vertically; rad >= 1 in an empty brick, so the
-    // quotient is a shift); sh 0, the cell itself (rad 1).
+    // 2, the brick of ci and s - 1 voxel layers beyond its far face, rad =
+    // s | shape << 6 ((s - 1) >> shape vertically; s >= 1 in an empty brick);
+    // sh 0, the cell itself (rad 1).
     __device__ __forceinline__ int exit_plane(int i, int ci, int sh, int rad) const {
         const int u = ci >> sh;
         int beyond = (rad - 1) << sh;   // cells beyond the unit's far face
-        if (sh == 2) beyond = i == 1 ? (int)((unsigned)(rad - 1) >> ((oct & 2u) ? 0 : kFlatYShift)) : rad - 1;
+        if (sh == 2) {
+            const int layers = (rad & 63) - 1;
+            beyond = i == 1 ? layers >> (rad >> 6) : layers;
+        }
         return r.pos[i] ? ((u + 1) << sh) + beyond : (u << sh) - beyond;
     }
 

@@ -124,18 +124,22 @@ __global__ void k_dist_pass(const unsigned long long* __restrict__ coarse, const
     }
 }
 
-// Brick level, in voxels.  Field o of brick b holds
-//     min(kVoxCap + 1, min over occupied voxels q ahead of b of max(dx, wy*dy, dz)),
-// wy = flat_y(o), where d_i is the number of voxel layers between b's far
-// face on axis i and q (0 when q lies within b's extent on that axis) and
-// "ahead" means q is not behind b's near face on any axis.  0 marks an
-// occupied brick; a value s >= 1 promises that b plus s - 1 layers beyond its
-// far faces across and (s - 1) / wy layers vertically holds no occupied
-// voxel.  Each pass coarsens one axis from voxels to bricks:
-//   x: X(bx, qy, qz), 2 fields: layers from brick bx's far x face to the first
-//      occupied voxel of row (qy, qz) (read from the mask words);
-//   y: Y(bx, by, qz), 4 fields: min over qy of max(wy*dy, X(bx, qy, qz));
-//   z: the brick field, 8 fields: min over qz of max(dz, Y(bx, by, qz)).
+// Brick level, in voxels.  With vertical weight w = 2^shape, brick b has
+//     s_w = min(kVoxCap + 1, min over occupied voxels q ahead of b of max(dx, w*dy, dz)),
+// where d_i is the number of voxel layers between b's far face on axis i and
+// q (0 when q lies within b's extent on that axis) and "ahead" means q is not
+// behind b's near face on any axis: b plus s_w - 1 layers beyond its far faces
+// across and (s_w - 1) / w layers vertically holds no occupied voxel (s_w = 0:
+// b is occupied).  Field o of b stores s_1 for the octants moving +y, and for
+// those moving -y the s_w | shape << 6 of the shape with the largest box
+// (box_score; the smallest weight on a tie).  Each pass coarsens one axis from
+// voxels to bricks:
+//   x: X(bx, qy, qz), 2 fields (x direction): layers from brick bx's far x face
+//      to the first occupied voxel of row (qy, qz) (read from the mask words);
+//   y: Y(bx, by, qz), kYFields fields (y_field: x and y direction, and for -y
+//      the shape): min over qy of max(w*dy, X(bx, qy, qz));
+//   z: the brick field, 8 fields: min over qz of max(dz, Y(bx, by, qz)), and
+//      the shape choice.
 // The intermediates are x-fastest arrays: X over (GX bricks, GY*4, GZ*4
 // voxels), Y over (GX, GY bricks, GZ*4 voxels).  Each pass covers a box of
 // its own output grid, [lo, lo + ext) clipped to the grid; with `d_cell`
@@ -151,6 +155,11 @@ struct BrickGrid {
     int CX, CY, CZ;   // chunks
     int GX, GY, GZ;   // bricks
 };
+
+// The y pass's fields: x direction xs, y direction ys (1: +y) and, for -y,
+// the box shape.
+constexpr int kYFields = 2 + 2 * kBoxShapes;
+__host__ __device__ constexpr int y_field(int xs, int ys, int shape) { return ys ? xs : 2 + xs + 2 * shape; }
 
 __device__ __forceinline__ bool box_cell(size_t lin, int3 lo, int3 ext, int3 g, int& x, int& y, int& z) {
     x = lo.x + (int)(lin % ext.x);
@@ -203,13 +212,14 @@ __global__ void k_bdist_y(const unsigned char* __restrict__ xf, unsigned char* _
         if (!d_cell[3]) return;
         lo = edit_origin(lo, d_cell, false, false, true);
     }
-    const unsigned v = blockIdx.y;   // bit 0: x direction, bit 1: y direction
-    const bool fwd = (v & 2u) != 0u;
-    const int wy = flat_y(v);
+    const int yi = (int)blockIdx.y;  // y_field(xs, ys, shape)
+    const bool fwd = yi < 2;
+    const int xs = fwd ? yi : (yi - 2) & 1, shape = fwd ? 0 : (yi - 2) >> 1;
+    const int wy = 1 << shape;
     const int Y = b.GY * 4;
     const int3 g = make_int3(b.GX, b.GY, b.GZ * 4);
-    xf += (size_t)(v & 1u) * ((size_t)b.GX * Y * g.z);
-    yf += (size_t)v * ((size_t)g.x * g.y * g.z);
+    xf += (size_t)xs * ((size_t)b.GX * Y * g.z);
+    yf += (size_t)yi * ((size_t)g.x * g.y * g.z);
     const size_t total = (size_t)ext.x * ext.y * ext.z;
     for (size_t lin = blockIdx.x * (size_t)blockDim.x + threadIdx.x; lin < total; lin += (size_t)gridDim.x * blockDim.x) {
         int bx, by, qz;
@@ -232,23 +242,36 @@ __global__ void k_bdist_z(const unsigned char* __restrict__ yf, unsigned char* _
         lo = edit_origin(lo, d_cell, false, false, false);
     }
     const unsigned v = blockIdx.y;   // the octant
-    const bool fwd = (v & 4u) != 0u;
+    const bool fwd = (v & 4u) != 0u, up = (v & 2u) != 0u;
+    const int xs = (int)(v & 1u);
     const int Z = b.GZ * 4;
     const int3 g = make_int3(b.GX, b.GY, b.GZ);
-    yf += (size_t)(v & 3u) * ((size_t)b.GX * b.GY * Z);
+    const size_t yfield = (size_t)b.GX * b.GY * Z;
     out += (size_t)v * stride;
     const size_t total = (size_t)ext.x * ext.y * ext.z;
     for (size_t lin = blockIdx.x * (size_t)blockDim.x + threadIdx.x; lin < total; lin += (size_t)gridDim.x * blockDim.x) {
         int bx, by, bz;
         if (!box_cell(lin, lo, ext, g, bx, by, bz)) continue;
-        int best = kVoxCap + 1;
-        for (int t = 0;; ++t) {
-            const int dz = max(0, t - 3);
-            const int qz = fwd ? 4 * bz + t : 4 * bz + 3 - t;
-            if (dz >= best || qz < 0 || qz >= Z) break;
-            best = min(best, max(dz, (int)yf[(size_t)bx + (size_t)g.x * ((size_t)by + (size_t)g.y * qz)]));
+        const size_t col = (size_t)bx + (size_t)g.x * (size_t)by;
+        unsigned char res = 0;
+        int best_score = -1;
+        for (int shape = 0; shape < (up ? 1 : kBoxShapes); ++shape) {
+            const unsigned char* f = yf + (size_t)y_field(xs, up ? 1 : 0, shape) * yfield;
+            int best = kVoxCap + 1;
+            for (int t = 0;; ++t) {
+                const int dz = max(0, t - 3);
+                const int qz = fwd ? 4 * bz + t : 4 * bz + 3 - t;
+                if (dz >= best || qz < 0 || qz >= Z) break;
+                best = min(best, max(dz, (int)f[col + (size_t)g.x * g.y * qz]));
+            }
+            if (best == 0) break;   // the brick is occupied
+            const int score = box_score(best, shape);
+            if (score > best_score) {
+                best_score = score;
+                res = (unsigned char)(best | (shape << 6));
+            }
         }
-        out[brick_index(bx, by, bz, b.CX, b.CY)] = (unsigned char)best;
+        out[brick_index(bx, by, bz, b.CX, b.CY)] = res;
     }
 }
 
@@ -284,11 +307,12 @@ void brick_passes(vt_world* w, cudaStream_t st, const int3 lo[3], const int3 ext
     const BrickGrid b = {w->cdim[0], w->cdim[1], w->cdim[2], w->cdim[0] * 8, w->cdim[1] * 8, w->cdim[2] * 8};
     const size_t nb = w->nchunks * kBricksPerChunk;
     unsigned char* xf = w->d_dtmp;             // 2 fields of 16 bytes per brick
-    unsigned char* yf = w->d_dtmp + 32 * nb;   // 4 fields of 4 bytes per brick
+    unsigned char* yf = w->d_dtmp + 32 * nb;   // kYFields fields of 4 bytes per brick
     if (volume(ext[0]))
         k_bdist_x<<<dim3(dist_blocks(volume(ext[0])), 2), kDistThreads, 0, st>>>(w->d_mask, xf, b, lo[0], ext[0], d_cell);
     if (volume(ext[1]))
-        k_bdist_y<<<dim3(dist_blocks(volume(ext[1])), 4), kDistThreads, 0, st>>>(xf, yf, b, lo[1], ext[1], d_cell);
+        k_bdist_y<<<dim3(dist_blocks(volume(ext[1])), kYFields), kDistThreads, 0, st>>>(xf, yf, b, lo[1], ext[1],
+                                                                                        d_cell);
     if (volume(ext[2]))
         k_bdist_z<<<dim3(dist_blocks(volume(ext[2])), 8), kDistThreads, 0, st>>>(yf, w->d_bdist, b, lo[2], ext[2],
                                                                                  d_cell, nb);
@@ -430,7 +454,7 @@ vt_status vt_world_create(vt_ctx* ctx, const vt_world_desc* desc, vt_world** out
         (e = vt::dev_alloc(&w->d_palette, 256 * sizeof(unsigned))) != cudaSuccess ||
         (e = vt::dev_alloc(&w->d_bdist, kOctants * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
         (e = vt::dev_alloc(&w->d_cdist, kOctants * (size_t)cdist_stride((unsigned)w->nchunks))) != cudaSuccess ||
-        (e = vt::dev_alloc(&w->d_dtmp, 48 * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
+        (e = vt::dev_alloc(&w->d_dtmp, (32 + 4 * kYFields) * w->nchunks * kBricksPerChunk)) != cudaSuccess ||
         (e = vt::dev_alloc(&w->d_ctmp, 6 * (size_t)cdist_stride((unsigned)w->nchunks))) != cudaSuccess ||
         (e = vt::dev_alloc(&w->d_edit, 4 * sizeof(int))) != cudaSuccess ||
         (e = vt::dev_alloc(&w->d_entities, kMaxEntities * 6 * sizeof(float))) != cudaSuccess ||
