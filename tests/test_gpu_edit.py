@@ -81,6 +81,42 @@ def test_distances_equal_independent_computation(vt, ctx, host_fields, dims, see
         w.close()
 
 
+def _shaped_world(dims, seed):
+    """A slab, an overhang, pillars and floating voxels: flat and tall empty
+    boxes, open space beyond the distance cap, ragged edges."""
+    X, Y, Z = dims
+    rng = np.random.default_rng(seed)
+    mats = np.zeros((Z, Y, X), np.uint8)
+    mats[:, : max(1, Y // 6), :] = 2                                  # ground slab
+    mats[Z // 4: Z // 2, Y // 2: Y // 2 + 2, X // 5: 4 * X // 5] = 3   # overhang
+    for _ in range(12):                                                # pillars
+        x, z = rng.integers(0, X), rng.integers(0, Z)
+        mats[z, : rng.integers(1, Y), x] = 4
+    mats[rng.random(mats.shape) < 0.0003] = 9                          # floating voxels
+    return mats
+
+
+@pytest.mark.parametrize("dims,seed", [((97, 41, 133), 21), ((300, 150, 40), 22), ((64, 7, 64), 23)])
+def test_distances_shaped_worlds(vt, ctx, host_fields, dims, seed):
+    """Brick and chunk fields against the independent host computation on
+    worlds whose empty boxes favour every box shape, with long reaches to the
+    cap and a world thinner than a brick's four layers would suggest."""
+    mats = _shaped_world(dims, seed)
+    w = vt.World(ctx, dims)
+    try:
+        w.upload_dense(mats)
+        b, c = w.distances()
+        hb, hc = host_fields(mats)
+        assert np.array_equal(c, hc)
+        for o in range(8):
+            bad = np.flatnonzero(b[o] != hb[o])
+            assert bad.size == 0, (o, bad[:8], b[o][bad[:8]], hb[o][bad[:8]])
+        down = b[[0, 1, 4, 5]]
+        assert ((down >> 6) > 0).any() and ((down >> 6) == 0).any() and ((b & 63) == 63).any()
+    finally:
+        w.close()
+
+
 def test_pick_matches_oracle(vt, oracle, ctx):
     desc = vt.gen_desc((160, 96, 128), scale=0.6, seed=4, trees=40, caves=True)
     mats = vt.gen_world(desc)
