@@ -204,6 +204,30 @@ def test_host_edits_update_distances_incrementally(vt, ctx):
         w.close()
 
 
+def test_corner_and_edge_edits_update_distances(vt, ctx):
+    """Single-voxel edits at the world's corners and edges, on chunk and brick
+    boundaries, in a world whose sides are not multiples of a brick: the
+    update boxes are clipped on every side and the result still equals a
+    fresh rebuild."""
+    X, Y, Z = 61, 45, 77
+    mats = _shaped_world((X, Y, Z), 31)
+    w = vt.World(ctx, (X, Y, Z))
+    try:
+        w.upload_dense(mats)
+        w.distances()
+        cells = [(x, y, z) for x in (0, X - 1) for y in (0, Y - 1) for z in (0, Z - 1)]
+        cells += [(31, 0, 0), (32, Y - 1, Z - 1), (0, 31, 40), (X - 1, 32, 3), (17, 44, 63), (60, 4, 64)]
+        for i, (x, y, z) in enumerate(cells):
+            m = 0 if mats[z, y, x] else 6
+            w.set(x, y, z, m)
+            mats[z, y, x] = m
+            if i % 3 == 2:
+                assert_same_distances(vt, ctx, w, mats)
+        assert_same_distances(vt, ctx, w, mats)
+    finally:
+        w.close()
+
+
 def test_edited_world_renders_like_fresh_upload(vt, oracle, ctx):
     desc = vt.gen_desc((96, 80, 112), scale=0.5, seed=31, trees=20)
     mats = vt.gen_world(desc)
