@@ -82,6 +82,33 @@ def test_trace_rays_kat(vt, oracle, ctx):
     w.close()
 
 
+def test_trace_rays_inside_origins_extreme_directions(vt, oracle, ctx):
+    """Origins inside the grid, on and near the one-cell margin below which a
+    walk starts in its own cell without the entry-box test, with direction
+    components from 1e-38 to 1e38 (reciprocals that overflow, underflow or
+    stay ordinary) and zero."""
+    dims = (64, 48, 72)
+    d = vt.gen_desc(dims, scale=0.5, seed=11, trees=8, caves=True)
+    mats = vt.gen_world(d)
+    w = make_world(vt, ctx, mats)
+    rng = np.random.default_rng(12)
+    n = 20000
+    o = rng.uniform([0.0, 0.0, 0.0], dims, (n, 3))
+    k = rng.random((n, 3))
+    edge = np.array(dims, np.float64)
+    o = np.where(k < 0.15, rng.choice([0.0, 0.5, 1.0, 1.0001, 0.9999], (n, 3)), o)
+    o = np.where(k > 0.85, edge - rng.choice([0.0, 0.5, 1.0, 1.0001, 0.9999], (n, 3)), o)
+    mags = np.array([0.0, 1e-38, 1e-30, 1e-8, 1.0, 1e8, 1e30, 1e38])
+    dirs = rng.normal(size=(n, 3))
+    dirs = np.where(rng.random((n, 3)) < 0.3, np.sign(dirs) * rng.choice(mags, (n, 3)), dirs)
+    o, dirs = np.ascontiguousarray(o, np.float32), np.ascontiguousarray(dirs, np.float32)
+    for steps in (1, 5000):
+        gpu = vt.trace_rays(ctx, w, o, dirs, steps)
+        compare(gpu, oracle.trace_rays(oracle.OracleWorld(mats), o, dirs, steps), rgb_tol=0)
+    assert (gpu["face"] != 0xFF).sum() > 3000
+    w.close()
+
+
 def test_far_origins_both_walker_variants(vt, oracle, ctx):
     """Origins on both sides of |o| = 2^20 (the walker's one-correction plane
     search below it, the correction loop above), aimed at the world, with
