@@ -124,7 +124,11 @@ typedef struct {
     const void* d_coarse;
 } vt_world_info;
 
-/* VoxelBrickmap.init (voxel.zig:32-39): an empty world. */
+/* VoxelBrickmap.init (voxel.zig:32-39): an empty world.  Device memory per
+ * 4^3 brick of the chunk-padded grid: 64 B materials, 8 B occupancy word,
+ * 8 B brick distances (one per direction octant) and 72 B kept for their
+ * incremental update, about 2.4 B per voxel in all (the 512x256x512 world
+ * takes 152 MiB, a 2048x256x2048 one 2.4 GiB). */
 vt_status vt_world_create(vt_ctx* ctx, const vt_world_desc* desc, vt_world** out);
 vt_status vt_world_destroy(vt_world* world);
 /* VoxelBrickmap.clear (voxel.zig:41-44). */
